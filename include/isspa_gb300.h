@@ -1,0 +1,227 @@
+/*
+ * isspa_gb300.h -- C ABI of the GB300 IS-SPA implicit-solvent MD force engine.
+ *
+ * Drop-in replacement for the per-step force path of mccullaghlab/ISSPA-Force-
+ * Cuda's total_force_cuda.x (src/total_force_cuda.cpp:102-154).  The reference
+ * binds C++ class references (atom&, isspa&, bond&, ...) and returns elapsed
+ * milliseconds; this ABI carries the same state behind an opaque engine
+ * handle, takes plain pointers and sizes, returns an int status (0 = OK,
+ * negative = error; never exit()) and reports milliseconds through an optional
+ * out-parameter.  Layouts follow the reference:
+ *   pos  float4 [n_atoms]: x, y, z, charge/sqrt(dielectric) (atom_class.h:31,
+ *        read_prmtop.cpp:125)
+ *   vel  float4 [n_atoms]: vx, vy, vz, mass with H masses reset to 12
+ *        (atom_class.h:37, read_prmtop.cpp:141-146)
+ *   force float4 [n_atoms]: fx, fy, fz, 0 (atom_class.h:33)
+ * Units are the reference's: Angstrom, kcal/mol, amu, Amber time units
+ * (dt = 0.002 ps * 20.455, config_class.cpp:123-124).
+ *
+ * Threading: one engine is driven by one host thread at a time; distinct
+ * engines are independent.  All work of an engine runs on its own CUDA stream.
+ */
+#ifndef ISSPA_GB300_H
+#define ISSPA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------- */
+#define ISSPA_OK 0
+#define ISSPA_ERR_ARG (-1)          /* invalid argument / size */
+#define ISSPA_ERR_IO (-2)           /* file could not be opened */
+#define ISSPA_ERR_PARSE (-3)        /* malformed prmtop / isspatop / config / rst7 */
+#define ISSPA_ERR_CUDA (-4)         /* CUDA runtime error */
+#define ISSPA_ERR_NOMEM (-5)        /* allocation failed or over the engine's memory cap */
+#define ISSPA_ERR_BOUNDS (-6)       /* a device-side bounds check tripped */
+#define ISSPA_ERR_TIMEOUT (-7)      /* a bounded device wait gave up */
+#define ISSPA_ERR_NONFINITE (-8)    /* a force or coordinate became NaN/Inf */
+#define ISSPA_ERR_UNSUPPORTED (-9)  /* input outside what the engine supports */
+#define ISSPA_ERR_STATE (-10)       /* call not valid in the engine's state */
+#define ISSPA_ERR_OVERFLOW (-11)    /* a force exceeded the fixed-point range */
+
+/* ---- system description (plain arrays) ---------------------------------- */
+/* One simulation window: everything the reference's atom / bond / angle / dih
+ * / isspa / us / config objects hold after setup (total_force_cuda.cpp:57-99).
+ * All indices are 0-based.  The engine copies what it needs at creation. */
+typedef struct isspa_system_desc {
+    int n_atoms;
+    const float *pos;            /* [n_atoms][4] */
+    const float *vel;            /* [n_atoms][4]; .w = mass (H -> 12) */
+    const float *raw_mass;       /* [n_atoms] prmtop masses (US mass fractions, us_class.cpp:147) */
+    /* Lennard-Jones (read_prmtop.cpp:151-203, :353-384) */
+    int n_lj_types;
+    const int *lj_type;          /* [n_atoms] */
+    const int *nb_parm_index;    /* [n_lj_types^2] index into lj_ab */
+    const float *lj_ab;          /* [n_lj_types*(n_lj_types+1)/2][2]: A, B */
+    /* exclusions (read_prmtop.cpp:167-186, :546-562): cumulative counts */
+    int excl_len;
+    const int *n_excl_cum;       /* [n_atoms] */
+    const int *excl_list;        /* [excl_len] */
+    /* bonded terms (read_prmtop.cpp:204-352, :386-545) */
+    int n_bonds;
+    const int *bond_atoms;       /* [n_bonds][3]: i, j, type */
+    int n_bond_types;
+    const float *bond_params;    /* [n_bond_types][2]: 2k, r0 */
+    int n_angles;
+    const int *angle_atoms;      /* [n_angles][4]: i, j, k, type */
+    int n_angle_types;
+    const float *angle_params;   /* [n_angle_types][2]: 2k, theta0 */
+    int n_dihs;
+    const int *dih_atoms;        /* [n_dihs][4]: i, j, +-k, +-l (sign flags as in Amber) */
+    const int *dih_types;        /* [n_dihs] */
+    int n_dih_types;
+    const float *dih_params;     /* [n_dih_types][4]: periodicity, k, phase, 0 */
+    const float *scaled14;       /* [n_dih_types][2]: SCEE, SCNB */
+    /* IS-SPA solvent model (isspa_class.cpp:45-178) */
+    const int *isspa_type;       /* [n_atoms] */
+    int n_isspa_types;
+    const float *rmax;           /* [n_isspa_types] */
+    int n_g, n_e, n_f;           /* rows per type of ISSPA_DENSITIES / _EFIELD / _FORCES */
+    const float *g_table;        /* [n_isspa_types][n_g] */
+    const float *e_table;        /* [n_isspa_types][n_e] */
+    const float *f_table;        /* [n_isspa_types][n_f] */
+    float g_r0, g_dr, e_r0, e_dr, f_r0, f_dr;
+    /* umbrella COM-distance restraint (us_class.cpp:13-158) */
+    int us_on;
+    int n_bias;
+    const int *bias_list;        /* [n_bias][2]: atom, group (0/1) */
+    float us_k, us_x0;
+    /* run parameters (config_class.cpp:14-133) */
+    int n_mc;
+    float box;
+    float kT;                    /* temperature * 0.00198717 */
+    float dt;                    /* Amber time units */
+    float pnu;                   /* Andersen collision probability per step */
+    uint64_t seed;
+} isspa_system_desc;
+
+/* ---- engine options ------------------------------------------------------ */
+typedef struct isspa_engine_options {
+    int isspa_terms;     /* bit mask: 1 multipole, 2 tabulated LJ, 4 CDD; 0 => all (7) */
+    int nonbond_terms;   /* bit mask: 1 LJ, 2 Coulomb, 4 IS-SPA correction; 0 => all (7) */
+    int use_graph;       /* isspa_step captures the step in a CUDA graph (default 1) */
+    int field_split;     /* atom-loop split per MC point in the field kernel; 0 => auto */
+    int force_chunk;     /* MC points per force-kernel work item; 0 => auto */
+    size_t mem_cap;      /* device bytes the engine may allocate; 0 => unlimited */
+} isspa_engine_options;
+
+typedef struct isspa_engine isspa_engine;
+typedef struct isspa_host_system isspa_host_system;
+
+const char *isspa_strerror(int status);
+void isspa_default_options(isspa_engine_options *opt);
+
+/* ---- input files (host side, no GPU needed) ------------------------------ */
+/* Parsed `key = value` run configuration (config_class.cpp:14-133). */
+typedef struct isspa_run_config {
+    char prmtop[512], isspa_prmtop[512], input_coord[512], input_vel[512], us_cfg[512];
+    char for_out[512], pos_out[512], vel_out[512], pos_rst_file[512], vel_rst_file[512];
+    int n_mc, n_steps, delta_write, seed, us, vel_rst;
+    int pnu_set;         /* 0 when the file gave no pnu (the reference leaves it uninitialised) */
+    float temperature;   /* K, as given */
+    float kT, dt, dt_ps, pnu, box, eps, cutoff;
+} isspa_run_config;
+
+/* Replaces config::initialize (config_class.cpp:14-133). */
+int isspa_read_run_config(const char *path, isspa_run_config *out);
+/* Reads prmtop (read_prmtop.cpp:10), isspatop (isspa_class.cpp:45), rst7
+ * positions (atom_class.cpp:76-115), velocities (:117-156) or a seeded
+ * Maxwell-Boltzmann draw (:53-64), and the US file (us_class.cpp:13-105).
+ * Relative paths resolve against base_dir when it is non-NULL. */
+int isspa_system_load(const isspa_run_config *cfg, const char *base_dir, isspa_host_system **out);
+int isspa_read_prmtop(const char *path, float eps, isspa_host_system **out);
+int isspa_read_isspatop(isspa_host_system *sys, const char *path);
+int isspa_read_rst7(isspa_host_system *sys, const char *path, int velocities);
+int isspa_read_us_config(isspa_host_system *sys, const char *path, char *cv_file_out, size_t cv_len);
+/* Points desc at the host system's arrays (valid until isspa_system_free). */
+int isspa_system_describe(const isspa_host_system *sys, isspa_system_desc *desc);
+int isspa_system_set_run(isspa_host_system *sys, int n_mc, float box, float kT, float dt,
+                         float pnu, uint64_t seed);
+void isspa_system_free(isspa_host_system *sys);
+
+/* ---- engine lifetime ----------------------------------------------------- */
+/* Creates an engine on the current CUDA device for n_windows independent
+ * windows (umbrella windows or replicas) that share one force field: the same
+ * LJ types/parameters, IS-SPA types/tables and n_mc.  n_windows == 1 is the
+ * plain drop-in path (replaces the setup of total_force_cuda.cpp:77-99). */
+int isspa_engine_create(const isspa_system_desc *windows, int n_windows,
+                        const isspa_engine_options *opt, isspa_engine **out);
+void isspa_engine_destroy(isspa_engine *e);
+int isspa_engine_info(const isspa_engine *e, int *n_windows, int *n_atoms_total,
+                      long long *n_points_total);
+
+/* ---- per-step force calls (reference names and order) -------------------- */
+/* Each call adds its forces into the engine's force accumulator, exactly as the
+ * reference kernels add into for_d.  With ms_out != NULL the call is timed
+ * with CUDA events and synchronises (like the reference wrappers); with NULL it
+ * is only enqueued on the engine stream. */
+int isspa_zero_forces(isspa_engine *e);                   /* cudaMemset(for_d), total_force_cuda.cpp:109 */
+int bond_force_cuda(isspa_engine *e, float *ms_out);      /* bond_force_cuda.cu:58-79 */
+int angle_force_cuda(isspa_engine *e, float *ms_out);     /* angle_force_cuda.cu:158-175 */
+int dih_force_cuda(isspa_engine *e, float *ms_out);       /* dih_force_cuda.cu:140-157 */
+int isspa_force_cuda(isspa_engine *e, float *ms_out);     /* isspa_force_cuda.cu:331-360 */
+int nonbond_force_cuda(isspa_engine *e, float *ms_out);   /* nonbond_force_cuda.cu:178-194 */
+int us_force_cuda(isspa_engine *e, float *ms_out);        /* us_force_cuda.cu:50-69 */
+int leapfrog_cuda(isspa_engine *e, float *ms_out);        /* leapfrog_cuda.cu:73-86; advances the step counter */
+
+/* Runs nsteps complete MD steps (zero, bonded, IS-SPA, nonbond, US, leapfrog)
+ * in the reference order, replayed from a captured CUDA graph. */
+int isspa_step(isspa_engine *e, int nsteps);
+/* Runs nsteps steps and returns their device time (CUDA events on the engine
+ * stream).  flush_bytes > 0 writes that many bytes of scratch between steps
+ * (outside the timed intervals) to evict L2. */
+int isspa_time_steps(isspa_engine *e, int nsteps, size_t flush_bytes, double *ms_total);
+int isspa_synchronize(isspa_engine *e);
+/* Sticky device status word (0 if nothing tripped); clears it when reset != 0. */
+int isspa_device_status(isspa_engine *e, int reset);
+
+/* ---- state transfer (host <-> device, synchronous) ----------------------- */
+int isspa_set_positions(isspa_engine *e, const float *pos4, int n_atoms_total);
+int isspa_get_positions(isspa_engine *e, float *pos4, int n_atoms_total);
+int isspa_set_velocities(isspa_engine *e, const float *vel4, int n_atoms_total);
+int isspa_get_velocities(isspa_engine *e, float *vel4, int n_atoms_total);
+/* Current contents of the force accumulator (float4, .w = 0). */
+int isspa_get_forces(isspa_engine *e, float *f4, int n_atoms_total);
+int isspa_set_step(isspa_engine *e, uint32_t step);
+int isspa_get_step(isspa_engine *e, uint32_t *step);
+/* Umbrella COM of both groups per window (double [n_windows][2][3]) and the
+ * collective variable |COM0 - COM1| (double [n_windows]) of the last us call. */
+int isspa_get_us_com(isspa_engine *e, double *com, double *cv);
+
+/* One MD step with host buffers: upload pos/vel, run one full step, download
+ * pos/vel/force.  This is the call a host-side driver makes per step. */
+int isspa_step_host(isspa_engine *e, const float *pos_in, const float *vel_in, float *pos_out,
+                    float *vel_out, float *force_out);
+
+/* ---- IS-SPA point-set access (parity with other implementations) -------- */
+/* Injects MC point positions (float [n_points_total][3]); subsequent
+ * isspa_force_cuda calls use them instead of generating Philox points, until
+ * isspa_clear_mc_points. */
+int isspa_set_mc_points(isspa_engine *e, const float *xyz, long long n_points_total);
+int isspa_clear_mc_points(isspa_engine *e);
+/* Per-point results of the last field pass: positions [P][3], density
+ * product w [P], in-range count n [P], mean field E [P][3], far field E0 [P][3]. */
+int isspa_get_point_fields(isspa_engine *e, float *xyz, float *w, int *n, float *efield,
+                           float *e0field, long long n_points_total);
+
+/* ---- neighbour and cell lists (neighborlist_cuda.cu, cell_list_cuda.cu) -- */
+/* All-pairs neighbour list of window 0 with r^2 < rnn^2, exclusions as the
+ * nonbond kernel; rows sorted ascending.  rows [n_atoms][max_per_atom], counts
+ * [n_atoms] (counts may exceed max_per_atom: rows then hold the first
+ * max_per_atom partners in ascending order). */
+int isspa_neighbor_list(isspa_engine *e, float rnn, int max_per_atom, int *rows, int *counts);
+/* Cell index of every atom of window 0 (cell_list_cuda.cu:27-29). */
+int isspa_cell_list(isspa_engine *e, float rc, const int ncell[3], int *cell_of_atom);
+
+/* Device FP32 throughput probe: runs a dependent-chain FMA kernel over the whole
+ * GPU and returns the measured TFLOP/s (FMA = 2 flops). */
+int isspa_measure_fp32_peak(double *tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ISSPA_GB300_H */

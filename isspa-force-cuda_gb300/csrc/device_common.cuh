@@ -1,0 +1,73 @@
+// device_common.cuh -- device-side layouts and helpers shared by the kernels.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace isspa {
+
+// IS-SPA constants, src/constants.h:6-13 of the reference (float literals).
+constexpr float kEp = 2.3473f;
+constexpr float kRho = 0.0075f;
+constexpr float kP0 = 4.173705894203977f;
+constexpr float kQ0 = 1.6899960102882601f;
+constexpr float kO0 = 9.3658298730779350f;
+constexpr float kPi = 3.1415926535f;
+
+// Fixed-point force accumulation: 32 fractional bits in a signed 64-bit word.
+// Integer addition is associative, so the summed force is bit-identical for
+// any order of the atomics.
+constexpr float kFixScale = 4294967296.0f;
+constexpr double kFixInv = 1.0 / 4294967296.0;
+constexpr float kFixLimit = 1.0e9f;  // |f| beyond this flags ISSPA_ERR_OVERFLOW
+
+// Device status bits (sticky, read by the host after a step).
+enum : int {
+    kStatusOverflow = 1,
+    kStatusNonFinite = 2,
+    kStatusBounds = 4,
+};
+
+// One window (umbrella window or replica) of a batch.
+struct WinDev {
+    int atom_off, n_atoms;     // global atom range
+    long long point_off;       // first MC point (global)
+    float box, hbox;
+    float kT, dt, pnu;
+    int bias_off, n_bias;      // umbrella atoms (global list range)
+    float us_k, us_x0;
+    int us_on;
+    int pad;
+};
+
+// Packed per-point results of the field pass, consumed by the force pass.
+struct PointsDev {
+    float4 *pos_s;   // x, y, z, w/n   (density per unit vtot)
+    float4 *ehat;    // unit mean field, 1/n
+    float4 *amp;     // p0<P1> w/n, q0<P2> w/n, o0<P3> w/n, 0
+    float4 *e0;      // E0/3 / n, 0
+};
+
+// Minimum image at most one box away (the reference's min_image): identical
+// result to `r > h ? r - L : (r < -h ? r + L : r)`.
+__device__ __forceinline__ float mimg(float r, float L, float h) {
+    return fabsf(r) > h ? r - copysignf(L, r) : r;
+}
+// Squared distance with a fixed operation sequence (no contraction freedom).
+__device__ __forceinline__ float dist2f(float x, float y, float z) {
+    return __fmaf_rn(z, z, __fmaf_rn(y, y, __fmul_rn(x, x)));
+}
+
+__device__ __forceinline__ long long to_fix(float v) { return __float2ll_rn(v * kFixScale); }
+
+__device__ __forceinline__ void fix_add3(unsigned long long *acc, float fx, float fy, float fz) {
+    atomicAdd(acc + 0, (unsigned long long)to_fix(fx));
+    atomicAdd(acc + 1, (unsigned long long)to_fix(fy));
+    atomicAdd(acc + 2, (unsigned long long)to_fix(fz));
+}
+
+__device__ __forceinline__ void check_force(int *status, float fx, float fy, float fz) {
+    float m = fmaxf(fabsf(fx), fmaxf(fabsf(fy), fabsf(fz)));
+    if (!(m <= kFixLimit)) atomicOr(status, (m != m || isinf(m)) ? kStatusNonFinite : kStatusOverflow);
+}
+
+}  // namespace isspa

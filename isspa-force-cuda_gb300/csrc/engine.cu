@@ -1,0 +1,1009 @@
+// engine.cu -- the engine object behind the C ABI: device memory layout,
+// work lists, the per-step call sequence and its CUDA-graph capture.
+//
+// Device layout (one engine = one batch of windows sharing a force field):
+//   pos, vel, force_out   float4 [Ntot]        (reference atom_class.h:31-38)
+//   facc                  int64  [Ntot][3]     fixed-point force accumulator
+//   atype                 int2   [Ntot]        LJ type, IS-SPA type
+//   atom_win              int    [Ntot]
+//   points (SoA float4)   [Ptot] x4            per-point field-pass results
+//   tables                g/E packed float4, force packed float2, LJ A/B float2
+// Windows are concatenated; every work list is built once at creation.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "host_system.h"
+#include "isspa_gb300.h"
+#include "kernels.h"
+
+using namespace isspa;
+
+namespace {
+
+constexpr int kStepsPerGraph = 8;
+
+struct Fail {
+    int code;
+};
+
+inline void ck(cudaError_t e) {
+    if (e != cudaSuccess) throw Fail{ISSPA_ERR_CUDA};
+}
+
+}  // namespace
+
+struct isspa_engine {
+    int device = 0;
+    cudaStream_t stream = nullptr, side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_a = nullptr, ev_b = nullptr;
+    isspa_engine_options opt{};
+    int n_windows = 0, n_atoms = 0, n_mc = 0;
+    long long n_points = 0;
+    std::vector<WinDev> win_h;
+    std::vector<void *> allocs;
+    size_t allocated = 0;
+
+    // device state
+    float4 *pos = nullptr, *vel = nullptr, *force_out = nullptr;
+    unsigned long long *facc = nullptr;
+    int2 *atype = nullptr;
+    int *atom_win = nullptr;
+    WinDev *win = nullptr;
+    float4 *gtab = nullptr;
+    float2 *ftab = nullptr, *ljab = nullptr;
+    float *rmax = nullptr, *vtot = nullptr;
+    int *excl_start = nullptr, *excl = nullptr;
+    int4 *field_tiles = nullptr;
+    int n_field_tiles = 0, field_split = 4;
+    int4 *force_items = nullptr;
+    int2 *force_chunks = nullptr;
+    int n_force_items = 0, force_chunk = 0;
+    int4 *nb_items = nullptr;
+    int *nb_nj = nullptr;
+    int n_nb_items = 0;
+    int4 *bonds = nullptr, *angles = nullptr, *dihs = nullptr;
+    float2 *bond_par = nullptr, *angle_par = nullptr, *sc14 = nullptr;
+    float4 *dih_par = nullptr;
+    int *dih_type = nullptr;
+    int n_bonds = 0, n_angles = 0, n_dihs = 0;
+    int *us_windows = nullptr;
+    int n_us = 0;
+    int2 *bias = nullptr;
+    float *mfrac = nullptr;
+    double *com = nullptr, *cv = nullptr;
+    PointsDev pts{};
+    float4 *raw_e = nullptr, *raw_e0 = nullptr;
+    float *pts_in = nullptr;
+    bool inject = false;
+    int *status = nullptr;
+    uint32_t *d_step = nullptr;
+    unsigned int *d_done = nullptr;
+    void *flush = nullptr;
+    size_t flush_bytes = 0;
+
+    // scalars shared by all windows
+    int n_itypes = 0, n_lj_types = 0, n_g = 0, n_e = 0, n_f = 0;
+    float g_r0 = 0, g_dr = 1, e_r0 = 0, e_dr = 1, f_r0 = 0, f_dr = 1, e0 = 0;
+    uint64_t seed = 0;
+
+    // graphs
+    cudaGraphExec_t graph1 = nullptr, graphN = nullptr;
+    std::vector<cudaEvent_t> tev;
+
+    template <typename T>
+    T *alloc(size_t n) {
+        size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
+        if (opt.mem_cap && allocated + bytes > opt.mem_cap) throw Fail{ISSPA_ERR_NOMEM};
+        void *p = nullptr;
+        cudaError_t e = cudaMalloc(&p, bytes);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            throw Fail{e == cudaErrorMemoryAllocation ? ISSPA_ERR_NOMEM : ISSPA_ERR_CUDA};
+        }
+        allocs.push_back(p);
+        allocated += bytes;
+        return static_cast<T *>(p);
+    }
+    template <typename T>
+    T *upload(const std::vector<T> &v) {
+        T *p = alloc<T>(v.size());
+        if (!v.empty()) ck(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+        return p;
+    }
+
+    ~isspa_engine() {
+        if (stream) cudaStreamSynchronize(stream);
+        if (graph1) cudaGraphExecDestroy(graph1);
+        if (graphN) cudaGraphExecDestroy(graphN);
+        for (auto ev : tev) cudaEventDestroy(ev);
+        for (cudaEvent_t ev : {ev_fork, ev_join, ev_a, ev_b})
+            if (ev) cudaEventDestroy(ev);
+        for (void *p : allocs) cudaFree(p);
+        if (side) cudaStreamDestroy(side);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    // ---------------------------------------------------------------- args
+    FieldArgs field_args() const {
+        FieldArgs a{};
+        a.pos = pos;
+        a.atype = atype;
+        a.win = win;
+        a.tiles = field_tiles;
+        a.n_tiles = n_field_tiles;
+        a.gtab = gtab;
+        a.rmax = rmax;
+        a.n_gbins = n_g - 1;
+        a.g_r0 = g_r0;
+        a.g_dr = g_dr;
+        a.g_inv = 1.0f / g_dr;
+        a.e_r0 = e_r0;
+        a.e_dr = e_dr;
+        a.e_inv = 1.0f / e_dr;
+        a.e0 = e0;
+        a.n_mc = n_mc;
+        a.seed_lo = (uint32_t)seed;
+        a.seed_hi = (uint32_t)(seed >> 32);
+        a.step_ptr = d_step;
+        a.pts_in = inject ? pts_in : nullptr;
+        a.out = pts;
+        a.raw_e = raw_e;
+        a.raw_e0 = raw_e0;
+        a.status = status;
+        return a;
+    }
+    ForceArgs force_args() const {
+        ForceArgs a{};
+        a.pos = pos;
+        a.atype = atype;
+        a.win = win;
+        a.items = force_items;
+        a.chunks = force_chunks;
+        a.n_items = n_force_items;
+        a.pts = pts;
+        a.ftab = ftab;
+        a.rmax = rmax;
+        a.vtot = vtot;
+        a.n_f = n_f;
+        a.f_r0 = f_r0;
+        a.f_dr = f_dr;
+        a.f_inv = 1.0f / f_dr;
+        a.terms = opt.isspa_terms;
+        a.facc = facc;
+        a.status = status;
+        return a;
+    }
+    NonbondArgs nonbond_args() const {
+        NonbondArgs a{};
+        a.pos = pos;
+        a.atype = atype;
+        a.atom_win = atom_win;
+        a.win = win;
+        a.items = nb_items;
+        a.items_nj = nb_nj;
+        a.n_items = n_nb_items;
+        a.ljab = ljab;
+        a.n_lj_types = n_lj_types;
+        a.rmax = rmax;
+        a.excl_start = excl_start;
+        a.excl = excl;
+        a.terms = opt.nonbond_terms;
+        a.facc = facc;
+        a.status = status;
+        return a;
+    }
+    BondedArgs bonded_args(int b, int an, int d) const {
+        BondedArgs a{};
+        a.pos = pos;
+        a.atom_win = atom_win;
+        a.win = win;
+        a.bonds = bonds;
+        a.n_bonds = n_bonds;
+        a.bond_par = bond_par;
+        a.angles = angles;
+        a.n_angles = n_angles;
+        a.angle_par = angle_par;
+        a.dihs = dihs;
+        a.dih_type = dih_type;
+        a.n_dihs = n_dihs;
+        a.dih_par = dih_par;
+        a.sc14 = sc14;
+        a.ljab = ljab;
+        a.atype = atype;
+        a.n_lj_types = n_lj_types;
+        a.do_bonds = b;
+        a.do_angles = an;
+        a.do_dihs = d;
+        a.facc = facc;
+        a.status = status;
+        return a;
+    }
+    UmbrellaArgs umbrella_args() const {
+        UmbrellaArgs a{};
+        a.pos = pos;
+        a.win = win;
+        a.us_windows = us_windows;
+        a.n_us_windows = n_us;
+        a.bias = bias;
+        a.mfrac = mfrac;
+        a.com = com;
+        a.cv = cv;
+        a.facc = facc;
+        a.status = status;
+        return a;
+    }
+    LeapfrogArgs leapfrog_args() const {
+        LeapfrogArgs a{};
+        a.pos = pos;
+        a.vel = vel;
+        a.force_out = force_out;
+        a.facc = facc;
+        a.atom_win = atom_win;
+        a.win = win;
+        a.n_atoms = n_atoms;
+        a.seed_lo = (uint32_t)seed;
+        a.seed_hi = (uint32_t)(seed >> 32);
+        a.step_ptr = d_step;
+        a.done_ptr = d_done;
+        a.status = status;
+        return a;
+    }
+
+    // ---------------------------------------------------------- sequences
+    void enqueue_isspa(cudaStream_t s, bool raw = false) {
+        launch_field(field_args(), field_split, raw, s);
+        launch_force(force_args(), s);
+    }
+    void enqueue_step_serial(cudaStream_t s) {
+        launch_bonded(bonded_args(1, 1, 1), s);
+        enqueue_isspa(s);
+        launch_nonbond(nonbond_args(), s);
+        launch_umbrella(umbrella_args(), s);
+        launch_leapfrog(leapfrog_args(), s);
+    }
+    // Step with the two independent chains (field->force and bonded, umbrella,
+    // nonbond) on forked streams; both add into the same accumulator.
+    void enqueue_step_forked() {
+        ck(cudaEventRecord(ev_fork, stream));
+        ck(cudaStreamWaitEvent(side, ev_fork, 0));
+        enqueue_isspa(stream);
+        launch_bonded(bonded_args(1, 1, 1), side);
+        launch_umbrella(umbrella_args(), side);
+        launch_nonbond(nonbond_args(), side);
+        ck(cudaEventRecord(ev_join, side));
+        ck(cudaStreamWaitEvent(stream, ev_join, 0));
+        launch_leapfrog(leapfrog_args(), stream);
+    }
+    cudaGraphExec_t capture(int nsteps) {
+        cudaGraph_t g = nullptr;
+        ck(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        try {
+            for (int k = 0; k < nsteps; ++k) enqueue_step_forked();
+        } catch (...) {
+            cudaStreamEndCapture(stream, &g);
+            if (g) cudaGraphDestroy(g);
+            throw;
+        }
+        ck(cudaStreamEndCapture(stream, &g));
+        cudaGraphExec_t ex = nullptr;
+        cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
+        cudaGraphDestroy(g);
+        ck(e);
+        return ex;
+    }
+    void invalidate_graphs() {
+        if (graph1) cudaGraphExecDestroy(graph1);
+        if (graphN) cudaGraphExecDestroy(graphN);
+        graph1 = graphN = nullptr;
+    }
+    void run_steps(int nsteps) {
+        if (!opt.use_graph) {
+            for (int k = 0; k < nsteps; ++k) enqueue_step_forked();
+            ck(cudaGetLastError());
+            return;
+        }
+        if (!graph1) graph1 = capture(1);
+        if (nsteps >= kStepsPerGraph && !graphN) graphN = capture(kStepsPerGraph);
+        int k = 0;
+        for (; k + kStepsPerGraph <= nsteps; k += kStepsPerGraph) ck(cudaGraphLaunch(graphN, stream));
+        for (; k < nsteps; ++k) ck(cudaGraphLaunch(graph1, stream));
+    }
+};
+
+namespace {
+
+// Effective exclusions of the reference's ascending-list scan
+// (nonbond_force_cuda.cu:72-108): partner e_k of atom a is found iff e_k > a
+// and no earlier entry of a's list is larger than e_k.
+void effective_exclusions(const isspa_host_system &s, std::vector<std::vector<int>> &nb) {
+    nb.assign(s.n_atoms, {});
+    for (int a = 0; a < s.n_atoms; ++a) {
+        int start = a == 0 ? 0 : s.n_excl_cum[a - 1], stop = s.n_excl_cum[a];
+        int run_max = INT32_MIN;
+        for (int k = start; k < stop; ++k) {
+            int e = s.excl_list[k];
+            if (e > a && e < s.n_atoms && e >= run_max) {
+                nb[a].push_back(e);
+                nb[e].push_back(a);
+            }
+            run_max = std::max(run_max, e);
+        }
+    }
+    for (auto &v : nb) {
+        std::sort(v.begin(), v.end());
+        v.erase(std::unique(v.begin(), v.end()), v.end());
+    }
+}
+
+bool same_force_field(const isspa_host_system &a, const isspa_host_system &b) {
+    return a.n_lj_types == b.n_lj_types && a.nb_parm_index == b.nb_parm_index && a.lj_ab == b.lj_ab &&
+           a.n_isspa_types == b.n_isspa_types && a.rmax == b.rmax && a.n_g == b.n_g && a.n_e == b.n_e &&
+           a.n_f == b.n_f && a.g_table == b.g_table && a.e_table == b.e_table && a.f_table == b.f_table &&
+           a.g_r0 == b.g_r0 && a.g_dr == b.g_dr && a.e_r0 == b.e_r0 && a.e_dr == b.e_dr &&
+           a.f_r0 == b.f_r0 && a.f_dr == b.f_dr && a.n_mc == b.n_mc && a.seed == b.seed;
+}
+
+void build(isspa_engine &E, const std::vector<isspa_host_system> &ws) {
+    const isspa_host_system &f0 = ws[0];
+    const int W = (int)ws.size();
+    E.n_windows = W;
+    E.n_mc = f0.n_mc;
+    E.seed = f0.seed;
+    E.n_itypes = f0.n_isspa_types;
+    E.n_lj_types = f0.n_lj_types;
+    E.n_g = f0.n_g;
+    E.n_e = f0.n_e;
+    E.n_f = f0.n_f;
+    E.g_r0 = f0.g_r0; E.g_dr = f0.g_dr;
+    E.e_r0 = f0.e_r0; E.e_dr = f0.e_dr;
+    E.f_r0 = f0.f_r0; E.f_dr = f0.f_dr;
+    // e0 = 3/(4 PI rho p0)*(1-1/ep), float as the reference macro (constants.h:13)
+    E.e0 = 3.0f / (4.0f * kPi * kRho * kP0) * (1.0f - 1.0f / kEp);
+
+    // ---- concatenated atoms ----
+    std::vector<float4> pos, vel;
+    std::vector<int2> atype;
+    std::vector<int> atom_win;
+    std::vector<int4> bonds, angles, dihs;
+    std::vector<int> dih_type;
+    std::vector<int2> bias;
+    std::vector<float> mfrac;
+    std::vector<int> us_windows;
+    std::vector<std::vector<int>> ex_all;
+    E.win_h.resize(W);
+    int off = 0;
+    long long poff = 0;
+    for (int w = 0; w < W; ++w) {
+        const isspa_host_system &s = ws[w];
+        WinDev &d = E.win_h[w];
+        d = WinDev{};
+        d.atom_off = off;
+        d.n_atoms = s.n_atoms;
+        d.point_off = poff;
+        d.box = s.box;
+        d.hbox = 0.5f * s.box;  // isspa_force_cuda.cu:394
+        d.kT = s.kT;
+        d.dt = s.dt;
+        d.pnu = s.pnu;
+        for (int i = 0; i < s.n_atoms; ++i) {
+            pos.push_back(make_float4(s.pos[4 * i], s.pos[4 * i + 1], s.pos[4 * i + 2], s.pos[4 * i + 3]));
+            vel.push_back(make_float4(s.vel[4 * i], s.vel[4 * i + 1], s.vel[4 * i + 2], s.vel[4 * i + 3]));
+            atype.push_back(make_int2(s.lj_type[i], s.isspa_type[i]));
+            atom_win.push_back(w);
+        }
+        for (size_t b = 0; b < s.bond_atoms.size() / 3; ++b)
+            bonds.push_back(make_int4(s.bond_atoms[3 * b] + off, s.bond_atoms[3 * b + 1] + off,
+                                      s.bond_atoms[3 * b + 2], 0));
+        for (size_t b = 0; b < s.angle_atoms.size() / 4; ++b)
+            angles.push_back(make_int4(s.angle_atoms[4 * b] + off, s.angle_atoms[4 * b + 1] + off,
+                                       s.angle_atoms[4 * b + 2] + off, s.angle_atoms[4 * b + 3]));
+        for (size_t b = 0; b < s.dih_types.size(); ++b) {
+            const int *a = &s.dih_atoms[4 * b];
+            const bool do14 = a[2] > 0 && a[3] > 0;  // dih_force_cuda.cu:60
+            dihs.push_back(make_int4(std::abs(a[0]) + off, std::abs(a[1]) + off, std::abs(a[2]) + off,
+                                     std::abs(a[3]) + off));
+            dih_type.push_back(s.dih_types[b] | (do14 ? 0x40000000 : 0));
+        }
+        if (s.us_on) {
+            d.us_on = 1;
+            d.bias_off = (int)bias.size();
+            d.n_bias = (int)s.bias_list.size() / 2;
+            d.us_k = s.us_k;
+            d.us_x0 = s.us_x0;
+            // us_class.cpp:136-152: mass fractions in float
+            float tot[2] = {0.f, 0.f};
+            for (int b = 0; b < d.n_bias; ++b) tot[s.bias_list[2 * b + 1]] += s.raw_mass[s.bias_list[2 * b]];
+            for (int b = 0; b < d.n_bias; ++b) {
+                int a = s.bias_list[2 * b], g = s.bias_list[2 * b + 1];
+                bias.push_back(make_int2(a + off, g));
+                mfrac.push_back(s.raw_mass[a] / tot[g]);
+            }
+            if (!(tot[0] > 0.f) || !(tot[1] > 0.f)) throw Fail{ISSPA_ERR_ARG};
+            us_windows.push_back(w);
+        }
+        std::vector<std::vector<int>> ex;
+        effective_exclusions(s, ex);
+        for (auto &v : ex) {
+            for (int &j : v) j += off;
+            ex_all.push_back(std::move(v));
+        }
+        off += s.n_atoms;
+        poff += (long long)s.n_atoms * s.n_mc;
+    }
+    E.n_atoms = off;
+    E.n_points = poff;
+    E.n_bonds = (int)bonds.size();
+    E.n_angles = (int)angles.size();
+    E.n_dihs = (int)dihs.size();
+    E.n_us = (int)us_windows.size();
+
+    // ---- force-field tables ----
+    const int nt = E.n_itypes;
+    const int pad = std::max({f0.n_g, f0.n_e, f0.n_f}) + 1;
+    auto padded = [&](const std::vector<float> &t) {
+        std::vector<float> p(t);
+        p.resize(t.size() + pad, 0.f);
+        return p;
+    };
+    std::vector<float> Gp = padded(f0.g_table), Ep = padded(f0.e_table), Fp = padded(f0.f_table);
+    std::vector<float4> gtab((size_t)nt * (f0.n_g - 1));
+    for (int t = 0; t < nt; ++t)
+        for (int b = 0; b < f0.n_g - 1; ++b) {
+            size_t gi = (size_t)t * f0.n_g + b, ei = (size_t)t * f0.n_e + b;
+            gtab[(size_t)t * (f0.n_g - 1) + b] = make_float4(Gp[gi], Gp[gi + 1], Ep[ei], Ep[ei + 1]);
+        }
+    std::vector<float2> ftab((size_t)nt * f0.n_f);
+    for (int t = 0; t < nt; ++t)
+        for (int b = 0; b < f0.n_f; ++b) {
+            size_t fi = (size_t)t * f0.n_f + b;
+            ftab[fi] = make_float2(Fp[fi], Fp[fi + 1]);
+        }
+    std::vector<float> vtot(nt);
+    for (int t = 0; t < nt; ++t) {
+        // isspa_class.cpp:41 (double arithmetic, stored as float)
+        double r = f0.rmax[t];
+        vtot[t] = (float)(4.0 / 3.0 * (double)kPi * r * r * r * 0.0074 / (double)(float)f0.n_mc);
+    }
+    const int nlj = f0.n_lj_types;
+    std::vector<float2> ljab((size_t)nlj * nlj);
+    for (int i = 0; i < nlj * nlj; ++i) {
+        int k = f0.nb_parm_index[i];
+        ljab[i] = make_float2(f0.lj_ab[2 * k], f0.lj_ab[2 * k + 1]);
+    }
+    std::vector<int> ex_start(E.n_atoms + 1, 0), ex_flat;
+    for (int i = 0; i < E.n_atoms; ++i) {
+        ex_start[i] = (int)ex_flat.size();
+        ex_flat.insert(ex_flat.end(), ex_all[i].begin(), ex_all[i].end());
+    }
+    ex_start[E.n_atoms] = (int)ex_flat.size();
+    std::vector<float2> bond_par, angle_par, sc14;
+    std::vector<float4> dih_par;
+    // per-window bonded parameter tables may differ: concatenate with offsets
+    {
+        int bo = 0, ao = 0, dofs = 0;
+        size_t bi = 0, ai = 0, di = 0;
+        for (int w = 0; w < W; ++w) {
+            const isspa_host_system &s = ws[w];
+            for (int t = 0; t < s.n_bond_types; ++t) bond_par.push_back(make_float2(s.bond_params[2 * t], s.bond_params[2 * t + 1]));
+            for (int t = 0; t < s.n_angle_types; ++t) angle_par.push_back(make_float2(s.angle_params[2 * t], s.angle_params[2 * t + 1]));
+            for (int t = 0; t < s.n_dih_types; ++t) {
+                dih_par.push_back(make_float4(s.dih_params[4 * t], s.dih_params[4 * t + 1], s.dih_params[4 * t + 2], 0.f));
+                sc14.push_back(make_float2(s.scaled14[2 * t], s.scaled14[2 * t + 1]));
+            }
+            for (size_t b = 0; b < s.bond_atoms.size() / 3; ++b) bonds[bi++].z += bo;
+            for (size_t b = 0; b < s.angle_atoms.size() / 4; ++b) angles[ai++].w += ao;
+            for (size_t b = 0; b < s.dih_types.size(); ++b) dih_type[di++] += dofs;
+            bo += s.n_bond_types;
+            ao += s.n_angle_types;
+            dofs += s.n_dih_types;
+        }
+    }
+
+    // ---- work lists ----
+    std::vector<int> order(W);
+    for (int w = 0; w < W; ++w) order[w] = w;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return ws[a].n_atoms > ws[b].n_atoms; });
+    // field tiles: S warps split the atom loop of 128/S points
+    const int slots = 2432;  // 152 SMs x 16 resident 128-thread blocks
+    auto tiles_for = [&](int S) {
+        long long n = 0;
+        for (int w = 0; w < W; ++w) n += ((long long)ws[w].n_atoms * E.n_mc + 128 / S - 1) / (128 / S);
+        return n;
+    };
+    int S = E.opt.field_split;
+    if (S != 1 && S != 2 && S != 4) S = tiles_for(1) >= slots ? 1 : (tiles_for(2) >= slots ? 2 : 4);
+    E.field_split = S;
+    std::vector<int4> ftiles;
+    const int tp = 128 / S;
+    for (int w : order) {
+        long long P = (long long)ws[w].n_atoms * E.n_mc;
+        for (long long p = 0; p < P; p += tp)
+            ftiles.push_back(make_int4(w, (int)(E.win_h[w].point_off + p), (int)std::min<long long>(tp, P - p), 0));
+    }
+    if (E.n_points > INT32_MAX) throw Fail{ISSPA_ERR_UNSUPPORTED};
+    E.n_field_tiles = (int)ftiles.size();
+    // force items: 128-atom tiles x point chunks
+    long long pairs = 0;
+    for (int w = 0; w < W; ++w) pairs += (long long)ws[w].n_atoms * ws[w].n_atoms * E.n_mc;
+    int C = E.opt.force_chunk;
+    if (C <= 0) {
+        long long target = 4 * (long long)slots;
+        long long c = pairs / (128LL * target);
+        c = std::max<long long>(128, std::min<long long>(8192, ((c + 127) / 128) * 128));
+        C = (int)c;
+    }
+    E.force_chunk = C;
+    std::vector<int4> fitems;
+    std::vector<int2> fchunks;
+    for (int w : order) {
+        const WinDev &d = E.win_h[w];
+        long long P = (long long)d.n_atoms * E.n_mc;
+        int c0 = (int)fchunks.size();
+        for (long long p = 0; p < P; p += C)
+            fchunks.push_back(make_int2((int)(d.point_off + p), (int)std::min<long long>(C, P - p)));
+        int nc = (int)fchunks.size() - c0;
+        for (int a = 0; a < d.n_atoms; a += 128)
+            for (int c = 0; c < nc; ++c)
+                fitems.push_back(make_int4(w, d.atom_off + a, std::min(128, d.n_atoms - a), c0 + c));
+    }
+    E.n_force_items = (int)fitems.size();
+    // nonbond items: 128 i-atoms x J partners
+    std::vector<int4> nitems;
+    std::vector<int> nnj;
+    long long npairs = 0;
+    for (int w = 0; w < W; ++w) npairs += (long long)ws[w].n_atoms * ws[w].n_atoms;
+    int J = (int)std::max<long long>(128, std::min<long long>(4096, ((npairs / (128LL * 608) + 127) / 128) * 128));
+    for (int w : order) {
+        const WinDev &d = E.win_h[w];
+        for (int a = 0; a < d.n_atoms; a += 128)
+            for (int j = 0; j < d.n_atoms; j += J) {
+                nitems.push_back(make_int4(w, d.atom_off + a, std::min(128, d.n_atoms - a), d.atom_off + j));
+                nnj.push_back(std::min(J, d.n_atoms - j));
+            }
+    }
+    E.n_nb_items = (int)nitems.size();
+
+    // ---- upload ----
+    E.pos = E.upload(pos);
+    E.vel = E.upload(vel);
+    E.force_out = E.alloc<float4>(E.n_atoms);
+    E.facc = E.alloc<unsigned long long>(3 * (size_t)E.n_atoms);
+    ck(cudaMemset(E.facc, 0, 3 * sizeof(unsigned long long) * E.n_atoms));
+    ck(cudaMemset(E.force_out, 0, sizeof(float4) * E.n_atoms));
+    E.atype = E.upload(atype);
+    E.atom_win = E.upload(atom_win);
+    E.win = E.upload(E.win_h);
+    E.gtab = E.upload(gtab);
+    E.ftab = E.upload(ftab);
+    E.rmax = E.upload(f0.rmax);
+    E.vtot = E.upload(vtot);
+    E.ljab = E.upload(ljab);
+    E.excl_start = E.upload(ex_start);
+    E.excl = E.upload(ex_flat);
+    E.field_tiles = E.upload(ftiles);
+    E.force_items = E.upload(fitems);
+    E.force_chunks = E.upload(fchunks);
+    E.nb_items = E.upload(nitems);
+    E.nb_nj = E.upload(nnj);
+    E.bonds = E.upload(bonds);
+    E.angles = E.upload(angles);
+    E.dihs = E.upload(dihs);
+    E.dih_type = E.upload(dih_type);
+    E.bond_par = E.upload(bond_par);
+    E.angle_par = E.upload(angle_par);
+    E.dih_par = E.upload(dih_par);
+    E.sc14 = E.upload(sc14);
+    E.us_windows = E.upload(us_windows);
+    E.bias = E.upload(bias);
+    E.mfrac = E.upload(mfrac);
+    E.com = E.alloc<double>(6 * (size_t)W);
+    E.cv = E.alloc<double>(W);
+    ck(cudaMemset(E.com, 0, sizeof(double) * 6 * W));
+    ck(cudaMemset(E.cv, 0, sizeof(double) * W));
+    E.pts.pos_s = E.alloc<float4>(E.n_points);
+    E.pts.ehat = E.alloc<float4>(E.n_points);
+    E.pts.amp = E.alloc<float4>(E.n_points);
+    E.pts.e0 = E.alloc<float4>(E.n_points);
+    E.status = E.alloc<int>(1);
+    E.d_step = E.alloc<uint32_t>(1);
+    E.d_done = E.alloc<unsigned int>(1);
+    ck(cudaMemset(E.status, 0, sizeof(int)));
+    ck(cudaMemset(E.d_step, 0, sizeof(uint32_t)));
+    ck(cudaMemset(E.d_done, 0, sizeof(unsigned int)));
+}
+
+int guard(isspa_engine *e) {
+    if (!e) return ISSPA_ERR_ARG;
+    return cudaSetDevice(e->device) == cudaSuccess ? ISSPA_OK : ISSPA_ERR_CUDA;
+}
+
+template <typename F>
+int run_guarded(F &&f) {
+    try {
+        f();
+        return cudaGetLastError() == cudaSuccess ? ISSPA_OK : ISSPA_ERR_CUDA;
+    } catch (const Fail &x) {
+        cudaGetLastError();
+        return x.code;
+    } catch (const std::bad_alloc &) {
+        return ISSPA_ERR_NOMEM;
+    }
+}
+
+// Times `f` with CUDA events on the engine stream when ms_out is given.
+template <typename F>
+int timed_call(isspa_engine *e, float *ms_out, F &&f) {
+    int rc = guard(e);
+    if (rc) return rc;
+    return run_guarded([&] {
+        if (ms_out) ck(cudaEventRecord(e->ev_a, e->stream));
+        f();
+        ck(cudaGetLastError());
+        if (ms_out) {
+            ck(cudaEventRecord(e->ev_b, e->stream));
+            ck(cudaEventSynchronize(e->ev_b));
+            ck(cudaEventElapsedTime(ms_out, e->ev_a, e->ev_b));
+        }
+    });
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *isspa_strerror(int s) {
+    switch (s) {
+        case ISSPA_OK: return "ok";
+        case ISSPA_ERR_ARG: return "invalid argument";
+        case ISSPA_ERR_IO: return "file could not be opened";
+        case ISSPA_ERR_PARSE: return "malformed input file";
+        case ISSPA_ERR_CUDA: return "CUDA runtime error";
+        case ISSPA_ERR_NOMEM: return "out of device memory (or over the engine memory cap)";
+        case ISSPA_ERR_BOUNDS: return "device bounds check tripped";
+        case ISSPA_ERR_TIMEOUT: return "bounded device wait timed out";
+        case ISSPA_ERR_NONFINITE: return "non-finite force or coordinate";
+        case ISSPA_ERR_UNSUPPORTED: return "input outside what the engine supports";
+        case ISSPA_ERR_STATE: return "call not valid in the engine state";
+        case ISSPA_ERR_OVERFLOW: return "force outside the fixed-point range";
+        default: return "unknown status";
+    }
+}
+
+void isspa_default_options(isspa_engine_options *o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof *o);
+    o->isspa_terms = 7;
+    o->nonbond_terms = 7;
+    o->use_graph = 1;
+}
+
+int isspa_engine_create(const isspa_system_desc *windows, int n_windows, const isspa_engine_options *opt,
+                        isspa_engine **out) {
+    if (!windows || n_windows <= 0 || !out) return ISSPA_ERR_ARG;
+    *out = nullptr;
+    std::vector<isspa_host_system> ws(n_windows);
+    for (int w = 0; w < n_windows; ++w) {
+        int rc = host_system_from_desc(windows[w], ws[w]);
+        if (rc) return rc;
+        if (w && !same_force_field(ws[0], ws[w])) return ISSPA_ERR_UNSUPPORTED;
+    }
+    std::unique_ptr<isspa_engine> e;
+    try {
+        e.reset(new isspa_engine());
+    } catch (...) {
+        return ISSPA_ERR_NOMEM;
+    }
+    if (opt) e->opt = *opt;
+    else isspa_default_options(&e->opt);
+    if (e->opt.isspa_terms == 0) e->opt.isspa_terms = 7;
+    if (e->opt.nonbond_terms == 0) e->opt.nonbond_terms = 7;
+    if (cudaGetDevice(&e->device) != cudaSuccess) {
+        cudaGetLastError();
+        return ISSPA_ERR_CUDA;
+    }
+    int rc = run_guarded([&] {
+        ck(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
+        ck(cudaStreamCreateWithFlags(&e->side, cudaStreamNonBlocking));
+        for (cudaEvent_t *ev : {&e->ev_fork, &e->ev_join})
+            ck(cudaEventCreateWithFlags(ev, cudaEventDisableTiming));
+        ck(cudaEventCreate(&e->ev_a));
+        ck(cudaEventCreate(&e->ev_b));
+        build(*e, ws);
+        ck(cudaDeviceSynchronize());
+    });
+    if (rc) return rc;
+    *out = e.release();
+    return ISSPA_OK;
+}
+
+void isspa_engine_destroy(isspa_engine *e) {
+    if (!e) return;
+    cudaSetDevice(e->device);
+    delete e;
+}
+
+int isspa_engine_info(const isspa_engine *e, int *nw, int *na, long long *np) {
+    if (!e) return ISSPA_ERR_ARG;
+    if (nw) *nw = e->n_windows;
+    if (na) *na = e->n_atoms;
+    if (np) *np = e->n_points;
+    return ISSPA_OK;
+}
+
+int isspa_zero_forces(isspa_engine *e) {
+    return timed_call(e, nullptr, [&] {
+        ck(cudaMemsetAsync(e->facc, 0, 3 * sizeof(unsigned long long) * e->n_atoms, e->stream));
+    });
+}
+
+int bond_force_cuda(isspa_engine *e, float *ms) {
+    return timed_call(e, ms, [&] { launch_bonded(e->bonded_args(1, 0, 0), e->stream); });
+}
+int angle_force_cuda(isspa_engine *e, float *ms) {
+    return timed_call(e, ms, [&] { launch_bonded(e->bonded_args(0, 1, 0), e->stream); });
+}
+int dih_force_cuda(isspa_engine *e, float *ms) {
+    return timed_call(e, ms, [&] { launch_bonded(e->bonded_args(0, 0, 1), e->stream); });
+}
+int isspa_force_cuda(isspa_engine *e, float *ms) {
+    return timed_call(e, ms, [&] { e->enqueue_isspa(e->stream); });
+}
+int nonbond_force_cuda(isspa_engine *e, float *ms) {
+    return timed_call(e, ms, [&] { launch_nonbond(e->nonbond_args(), e->stream); });
+}
+int us_force_cuda(isspa_engine *e, float *ms) {
+    return timed_call(e, ms, [&] { launch_umbrella(e->umbrella_args(), e->stream); });
+}
+int leapfrog_cuda(isspa_engine *e, float *ms) {
+    return timed_call(e, ms, [&] { launch_leapfrog(e->leapfrog_args(), e->stream); });
+}
+
+int isspa_step(isspa_engine *e, int nsteps) {
+    if (nsteps < 0) return ISSPA_ERR_ARG;
+    return timed_call(e, nullptr, [&] { e->run_steps(nsteps); });
+}
+
+int isspa_time_steps(isspa_engine *e, int nsteps, size_t flush_bytes, double *ms_total) {
+    if (nsteps <= 0 || !ms_total) return ISSPA_ERR_ARG;
+    int rc = guard(e);
+    if (rc) return rc;
+    return run_guarded([&] {
+        if (flush_bytes && flush_bytes != e->flush_bytes) {
+            if (e->flush) {
+                cudaFree(e->flush);
+                e->flush = nullptr;
+            }
+            ck(cudaMalloc(&e->flush, flush_bytes));
+            e->flush_bytes = flush_bytes;
+        }
+        while ((int)e->tev.size() < 2 * nsteps) {
+            cudaEvent_t ev;
+            ck(cudaEventCreate(&ev));
+            e->tev.push_back(ev);
+        }
+        for (int k = 0; k < nsteps; ++k) {
+            if (flush_bytes) ck(cudaMemsetAsync(e->flush, k & 0xff, flush_bytes, e->stream));
+            ck(cudaEventRecord(e->tev[2 * k], e->stream));
+            e->run_steps(1);
+            ck(cudaEventRecord(e->tev[2 * k + 1], e->stream));
+        }
+        ck(cudaStreamSynchronize(e->stream));
+        double tot = 0.0;
+        for (int k = 0; k < nsteps; ++k) {
+            float ms = 0.f;
+            ck(cudaEventElapsedTime(&ms, e->tev[2 * k], e->tev[2 * k + 1]));
+            tot += ms;
+        }
+        *ms_total = tot;
+    });
+}
+
+int isspa_synchronize(isspa_engine *e) {
+    int rc = guard(e);
+    if (rc) return rc;
+    if (cudaStreamSynchronize(e->stream) != cudaSuccess) {
+        cudaGetLastError();
+        return ISSPA_ERR_CUDA;
+    }
+    return isspa_device_status(e, 0);
+}
+
+int isspa_device_status(isspa_engine *e, int reset) {
+    int rc = guard(e);
+    if (rc) return rc;
+    int st = 0;
+    if (cudaMemcpy(&st, e->status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return ISSPA_ERR_CUDA;
+    if (reset) cudaMemset(e->status, 0, sizeof(int));
+    if (st & kStatusNonFinite) return ISSPA_ERR_NONFINITE;
+    if (st & kStatusOverflow) return ISSPA_ERR_OVERFLOW;
+    if (st & kStatusBounds) return ISSPA_ERR_BOUNDS;
+    return ISSPA_OK;
+}
+
+static int copy_state(isspa_engine *e, void *dst, const void *src, size_t bytes, cudaMemcpyKind k) {
+    int rc = guard(e);
+    if (rc) return rc;
+    return run_guarded([&] {
+        ck(cudaMemcpyAsync(dst, src, bytes, k, e->stream));
+        ck(cudaStreamSynchronize(e->stream));
+    });
+}
+
+int isspa_set_positions(isspa_engine *e, const float *p, int n) {
+    if (!e || !p || n != e->n_atoms) return ISSPA_ERR_ARG;
+    return copy_state(e, e->pos, p, sizeof(float4) * n, cudaMemcpyHostToDevice);
+}
+int isspa_get_positions(isspa_engine *e, float *p, int n) {
+    if (!e || !p || n != e->n_atoms) return ISSPA_ERR_ARG;
+    return copy_state(e, p, e->pos, sizeof(float4) * n, cudaMemcpyDeviceToHost);
+}
+int isspa_set_velocities(isspa_engine *e, const float *p, int n) {
+    if (!e || !p || n != e->n_atoms) return ISSPA_ERR_ARG;
+    return copy_state(e, e->vel, p, sizeof(float4) * n, cudaMemcpyHostToDevice);
+}
+int isspa_get_velocities(isspa_engine *e, float *p, int n) {
+    if (!e || !p || n != e->n_atoms) return ISSPA_ERR_ARG;
+    return copy_state(e, p, e->vel, sizeof(float4) * n, cudaMemcpyDeviceToHost);
+}
+
+int isspa_get_forces(isspa_engine *e, float *f4, int n) {
+    if (!e || !f4 || n != e->n_atoms) return ISSPA_ERR_ARG;
+    std::vector<long long> acc(3 * (size_t)n);
+    int rc = copy_state(e, acc.data(), e->facc, sizeof(long long) * 3 * n, cudaMemcpyDeviceToHost);
+    if (rc) return rc;
+    for (int i = 0; i < n; ++i) {
+        for (int k = 0; k < 3; ++k) f4[4 * i + k] = (float)((double)acc[3 * i + k] * kFixInv);
+        f4[4 * i + 3] = 0.f;
+    }
+    return ISSPA_OK;
+}
+
+int isspa_set_step(isspa_engine *e, uint32_t step) {
+    if (!e) return ISSPA_ERR_ARG;
+    return copy_state(e, e->d_step, &step, sizeof step, cudaMemcpyHostToDevice);
+}
+int isspa_get_step(isspa_engine *e, uint32_t *step) {
+    if (!e || !step) return ISSPA_ERR_ARG;
+    return copy_state(e, step, e->d_step, sizeof *step, cudaMemcpyDeviceToHost);
+}
+
+int isspa_get_us_com(isspa_engine *e, double *com, double *cv) {
+    if (!e) return ISSPA_ERR_ARG;
+    int rc = ISSPA_OK;
+    if (com) rc = copy_state(e, com, e->com, sizeof(double) * 6 * e->n_windows, cudaMemcpyDeviceToHost);
+    if (!rc && cv) rc = copy_state(e, cv, e->cv, sizeof(double) * e->n_windows, cudaMemcpyDeviceToHost);
+    return rc;
+}
+
+int isspa_step_host(isspa_engine *e, const float *pin, const float *vin, float *pout, float *vout, float *fout) {
+    int rc = guard(e);
+    if (rc) return rc;
+    const size_t b = sizeof(float4) * e->n_atoms;
+    return run_guarded([&] {
+        if (pin) ck(cudaMemcpyAsync(e->pos, pin, b, cudaMemcpyHostToDevice, e->stream));
+        if (vin) ck(cudaMemcpyAsync(e->vel, vin, b, cudaMemcpyHostToDevice, e->stream));
+        e->run_steps(1);
+        if (pout) ck(cudaMemcpyAsync(pout, e->pos, b, cudaMemcpyDeviceToHost, e->stream));
+        if (vout) ck(cudaMemcpyAsync(vout, e->vel, b, cudaMemcpyDeviceToHost, e->stream));
+        if (fout) ck(cudaMemcpyAsync(fout, e->force_out, b, cudaMemcpyDeviceToHost, e->stream));
+        ck(cudaStreamSynchronize(e->stream));
+    });
+}
+
+int isspa_set_mc_points(isspa_engine *e, const float *xyz, long long n) {
+    if (!e || !xyz || n != e->n_points) return ISSPA_ERR_ARG;
+    int rc = guard(e);
+    if (rc) return rc;
+    rc = run_guarded([&] {
+        if (!e->pts_in) e->pts_in = e->alloc<float>(3 * (size_t)e->n_points);
+        ck(cudaMemcpy(e->pts_in, xyz, sizeof(float) * 3 * n, cudaMemcpyHostToDevice));
+    });
+    if (!rc && !e->inject) {
+        e->inject = true;
+        e->invalidate_graphs();
+    }
+    return rc;
+}
+
+int isspa_clear_mc_points(isspa_engine *e) {
+    if (!e) return ISSPA_ERR_ARG;
+    if (e->inject) {
+        e->inject = false;
+        e->invalidate_graphs();
+    }
+    return ISSPA_OK;
+}
+
+int isspa_get_point_fields(isspa_engine *e, float *xyz, float *w, int *n, float *ef, float *e0f, long long np) {
+    if (!e || np != e->n_points) return ISSPA_ERR_ARG;
+    int rc = guard(e);
+    if (rc) return rc;
+    return run_guarded([&] {
+        if (!e->raw_e) {
+            e->raw_e = e->alloc<float4>(e->n_points);
+            e->raw_e0 = e->alloc<float4>(e->n_points);
+        }
+        launch_field(e->field_args(), e->field_split, true, e->stream);
+        ck(cudaGetLastError());
+        std::vector<float4> a(e->n_points), b(e->n_points), c(e->n_points);
+        ck(cudaMemcpyAsync(a.data(), e->raw_e, sizeof(float4) * np, cudaMemcpyDeviceToHost, e->stream));
+        ck(cudaMemcpyAsync(b.data(), e->raw_e0, sizeof(float4) * np, cudaMemcpyDeviceToHost, e->stream));
+        ck(cudaMemcpyAsync(c.data(), e->pts.pos_s, sizeof(float4) * np, cudaMemcpyDeviceToHost, e->stream));
+        ck(cudaStreamSynchronize(e->stream));
+        for (long long p = 0; p < np; ++p) {
+            if (xyz) { xyz[3 * p] = c[p].x; xyz[3 * p + 1] = c[p].y; xyz[3 * p + 2] = c[p].z; }
+            if (w) w[p] = a[p].w;
+            if (n) n[p] = (int)b[p].w;
+            if (ef) { ef[3 * p] = a[p].x; ef[3 * p + 1] = a[p].y; ef[3 * p + 2] = a[p].z; }
+            if (e0f) { e0f[3 * p] = b[p].x; e0f[3 * p + 1] = b[p].y; e0f[3 * p + 2] = b[p].z; }
+        }
+    });
+}
+
+int isspa_neighbor_list(isspa_engine *e, float rnn, int max_per_atom, int *rows, int *counts) {
+    if (!e || !rows || !counts || max_per_atom <= 0 || !(rnn > 0.f)) return ISSPA_ERR_ARG;
+    int rc = guard(e);
+    if (rc) return rc;
+    const WinDev &d = e->win_h[0];
+    int *d_rows = nullptr, *d_counts = nullptr;
+    rc = run_guarded([&] {
+        ck(cudaMalloc(&d_rows, sizeof(int) * (size_t)d.n_atoms * max_per_atom));
+        ck(cudaMalloc(&d_counts, sizeof(int) * d.n_atoms));
+        ck(cudaMemsetAsync(d_rows, 0xff, sizeof(int) * (size_t)d.n_atoms * max_per_atom, e->stream));
+        ListArgs a{};
+        a.pos = e->pos;
+        a.excl_start = e->excl_start;
+        a.excl = e->excl;
+        a.atom_off = d.atom_off;
+        a.n_atoms = d.n_atoms;
+        a.box = d.box;
+        a.hbox = d.hbox;
+        a.rnn2 = rnn * rnn;
+        a.max_per_atom = max_per_atom;
+        a.rows = d_rows;
+        a.counts = d_counts;
+        launch_neighbor_list(a, e->stream);
+        ck(cudaGetLastError());
+        ck(cudaMemcpyAsync(rows, d_rows, sizeof(int) * (size_t)d.n_atoms * max_per_atom, cudaMemcpyDeviceToHost, e->stream));
+        ck(cudaMemcpyAsync(counts, d_counts, sizeof(int) * d.n_atoms, cudaMemcpyDeviceToHost, e->stream));
+        ck(cudaStreamSynchronize(e->stream));
+    });
+    if (d_rows) cudaFree(d_rows);
+    if (d_counts) cudaFree(d_counts);
+    return rc;
+}
+
+int isspa_cell_list(isspa_engine *e, float rc_len, const int ncell[3], int *cell) {
+    if (!e || !ncell || !cell || !(rc_len > 0.f)) return ISSPA_ERR_ARG;
+    int rc = guard(e);
+    if (rc) return rc;
+    const WinDev &d = e->win_h[0];
+    int *d_cell = nullptr;
+    rc = run_guarded([&] {
+        ck(cudaMalloc(&d_cell, sizeof(int) * d.n_atoms));
+        launch_cell_index(e->pos, d.atom_off, d.n_atoms, rc_len, make_int3(ncell[0], ncell[1], ncell[2]), d_cell,
+                          e->stream);
+        ck(cudaGetLastError());
+        ck(cudaMemcpyAsync(cell, d_cell, sizeof(int) * d.n_atoms, cudaMemcpyDeviceToHost, e->stream));
+        ck(cudaStreamSynchronize(e->stream));
+    });
+    if (d_cell) cudaFree(d_cell);
+    return rc;
+}
+
+int isspa_measure_fp32_peak(double *tflops) {
+    if (!tflops) return ISSPA_ERR_ARG;
+    double v = measure_fp32_peak_tflops();
+    if (v <= 0) return ISSPA_ERR_CUDA;
+    *tflops = v;
+    return ISSPA_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,335 @@
+// k_isspa.cu -- IS-SPA solvent kernels for sm_103a.
+//
+// Replaces the reference's three-kernel IS-SPA pass (src/isspa_force_cuda.cu:
+// 73-107 MC points, :110-206 field, :208-327 force) with two kernels:
+//
+//  field:  one thread-column per MC point.  The point is generated in the
+//          prologue from Philox counters (no stored RNG state), every atom of
+//          the point's window is streamed through shared memory, and the
+//          density product, in-range count, mean field and far field are
+//          reduced in registers and combined across the S warps that split the
+//          atom loop in a fixed order.  One writer per point: no atomics, no
+//          racy re-read of the density (the reference's atomicMul, :195).
+//          The per-point prologue of the reference's force kernel (|E|, unit
+//          field, Langevin averages, 1/n; :253-273) is computed here once per
+//          point instead of once per (atom, point) pair.
+//  force:  one thread per receiving atom; MC points are streamed through shared
+//          memory in chunks (broadcast reads); per-thread FP32 partial sums are
+//          flushed once per chunk into int64 fixed-point accumulators, so the
+//          final force is independent of scheduling order.
+#include <cuda_runtime.h>
+
+#include "kernels.h"
+#include "philox.h"
+
+namespace isspa {
+
+namespace {
+
+constexpr int kFieldThreads = 128;
+constexpr int kForceThreads = 128;
+
+// <P1>, <P2>, <P3> of a Langevin dipole in a field of magnitude x.  Below 5
+// the ratios i_l/i_(l-1) of modified spherical Bessel functions are taken from
+// their backward continued fraction r_l = x / (2l+1 + x r_(l+1)) (all terms
+// positive, no cancellation); above, the closed forms of the reference
+// (isspa_force_cuda.cu:270-273, 283, 287) are exact to float rounding.
+__device__ __forceinline__ void langevin3(float x, float &p1, float &p2, float &p3) {
+    if (x < 5.0f) {
+        float r = 0.0f, r2 = 0.0f, r3 = 0.0f;
+#pragma unroll
+        for (int l = 12; l >= 1; --l) {
+            r = __fdiv_rn(x, (float)(2 * l + 1) + x * r);
+            if (l == 3) r3 = r;
+            if (l == 2) r2 = r;
+        }
+        p1 = r;
+        p2 = r * r2;
+        p3 = p2 * r3;
+    } else {
+        const float c = 1.0f / tanhf(x);
+        const float ix = 1.0f / x;
+        const float ix2 = ix * ix;
+        p1 = c - ix;
+        p2 = 1.0f + 3.0f * ix2 - 3.0f * c * ix;
+        p3 = (1.0f + 15.0f * ix2) * c - 6.0f * ix - 15.0f * ix2 * ix;
+    }
+}
+
+// MC point p (index within its window) of `owner` at position xa with radius
+// rm: uniform in the ball r^2 < 0.99 (isspa_force_cuda.cu:92-100).
+__device__ __forceinline__ void mc_point(uint32_t p, uint32_t window, uint32_t step, uint32_t k0,
+                                         uint32_t k1, float4 xa, float rm, float &px, float &py,
+                                         float &pz) {
+    float mx = 0.5f, my = 0.0f, mz = 0.0f;
+    for (uint32_t att = 0; att < 64u; ++att) {
+        u32x4 o = philox4x32_10(u32x4{p, att, step, (window << 8) | 0u}, k0, k1);
+        float x = __fmaf_rn(2.0f, u01(o.x), -1.0f);
+        float y = __fmaf_rn(2.0f, u01(o.y), -1.0f);
+        float z = __fmaf_rn(2.0f, u01(o.z), -1.0f);
+        if (dist2f(x, y, z) < 0.99f) {
+            mx = x; my = y; mz = z;
+            break;
+        }
+    }
+    px = __fmaf_rn(mx, rm, xa.x);
+    py = __fmaf_rn(my, rm, xa.y);
+    pz = __fmaf_rn(mz, rm, xa.z);
+}
+
+template <int S, bool GEN, bool RAW>
+__global__ void __launch_bounds__(kFieldThreads) field_kernel(FieldArgs a) {
+    constexpr int kGroups = 4 / S;  // groups of 32 points per block
+    __shared__ float4 s_atom[kFieldThreads];
+    __shared__ int s_row[kFieldThreads];
+    __shared__ float s_red[S > 1 ? 8 : 1][kFieldThreads];
+
+    const int4 tile = a.tiles[blockIdx.x];
+    const WinDev W = a.win[tile.x];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int grp = warp / S, sp = warp % S;
+    const int slot = grp * 32 + lane;
+    const bool valid = slot < tile.z;
+    const long long pg = tile.y + (valid ? slot : tile.z - 1);  // global point
+    const long long pw = pg - W.point_off;                        // point within window
+    const int owner = W.atom_off + (int)(pw / a.n_mc);
+    const float4 xo = a.pos[owner];
+    const float rm = __ldg(a.rmax + a.atype[owner].y);
+    const float rm2 = __fmul_rn(rm, rm);
+    const float L = W.box, h = W.hbox;
+
+    float px, py, pz;
+    if (GEN) {
+        mc_point((uint32_t)pw, (uint32_t)tile.x, *a.step_ptr, a.seed_lo, a.seed_hi, xo, rm, px, py, pz);
+    } else {
+        px = a.pts_in[3 * pg + 0];
+        py = a.pts_in[3 * pg + 1];
+        pz = a.pts_in[3 * pg + 2];
+    }
+
+    float w = 1.0f;
+    int n = 0;
+    float ex = 0.f, ey = 0.f, ez = 0.f, fx = 0.f, fy = 0.f, fz = 0.f;
+    const float g_r0 = a.g_r0, g_dr = a.g_dr, g_inv = a.g_inv;
+    const float e_r0 = a.e_r0, e_dr = a.e_dr, e_inv = a.e_inv;
+    const int nb = a.n_gbins;
+
+    for (int j0 = 0; j0 < W.n_atoms; j0 += kFieldThreads) {
+        const int jn = min(kFieldThreads, W.n_atoms - j0);
+        __syncthreads();
+        if (threadIdx.x < jn) {
+            const int j = W.atom_off + j0 + threadIdx.x;
+            float4 xj = a.pos[j];
+            xj.w = a.e0 * xj.w;  // e0*q (isspa_force_cuda.cu:179, :183)
+            s_atom[threadIdx.x] = xj;
+            s_row[threadIdx.x] = a.atype[j].y * nb;
+        }
+        __syncthreads();
+#pragma unroll 2
+        for (int k = sp; k < jn; k += S) {
+            const float4 xj = s_atom[k];
+            const float rx = mimg(px - xj.x, L, h);
+            const float ry = mimg(py - xj.y, L, h);
+            const float rz = mimg(pz - xj.z, L, h);
+            const float d2 = dist2f(rx, ry, rz);
+            const float ri = rsqrtf(d2);
+            const float c = xj.w * (ri * ri * ri);
+            ex = fmaf(-c, rx, ex);
+            ey = fmaf(-c, ry, ey);
+            ez = fmaf(-c, rz, ez);
+            if (d2 <= rm2) {  // inside rmax of the owner's type (:154)
+                ++n;
+                const float dist = __fsqrt_rn(d2);
+                const int bin = (int)__fmul_rn(__fsub_rn(dist, g_r0), g_inv);
+                if (bin < 0) {
+                    w = 0.0f;
+                } else if (bin < nb) {
+                    const float4 t = __ldg(a.gtab + s_row[k] + bin);
+                    const float fg = (dist - fmaf((float)bin, g_dr, g_r0)) * g_inv;
+                    w *= fmaf(fg, t.y - t.x, t.x);
+                    const float fe = (dist - fmaf((float)bin, e_dr, e_r0)) * e_inv;
+                    const float et = fmaf(fe, t.w - t.z, t.z) * ri;
+                    ex = fmaf(et, rx, ex);
+                    ey = fmaf(et, ry, ey);
+                    ez = fmaf(et, rz, ez);
+                }
+            } else {
+                fx = fmaf(-c, rx, fx);
+                fy = fmaf(-c, ry, fy);
+                fz = fmaf(-c, rz, fz);
+            }
+        }
+    }
+
+    if (S > 1) {
+        s_red[0][threadIdx.x] = w;
+        s_red[1][threadIdx.x] = __int_as_float(n);
+        s_red[2][threadIdx.x] = ex;
+        s_red[3][threadIdx.x] = ey;
+        s_red[4][threadIdx.x] = ez;
+        s_red[5][threadIdx.x] = fx;
+        s_red[6][threadIdx.x] = fy;
+        s_red[7][threadIdx.x] = fz;
+        __syncthreads();
+        if (sp != 0) return;
+#pragma unroll
+        for (int s = 1; s < S; ++s) {
+            const int o = (grp * S + s) * 32 + lane;
+            w *= s_red[0][o];
+            n += __float_as_int(s_red[1][o]);
+            ex += s_red[2][o];
+            ey += s_red[3][o];
+            ez += s_red[4][o];
+            fx += s_red[5][o];
+            fy += s_red[6][o];
+            fz += s_red[7][o];
+        }
+    }
+    if (!valid) return;
+
+    if (RAW) {
+        a.raw_e[pg] = make_float4(ex, ey, ez, w);
+        a.raw_e0[pg] = make_float4(fx, fy, fz, (float)n);
+    }
+    if (n <= 0) {  // cannot happen: the owner itself is always in range
+        atomicOr(a.status, kStatusBounds);
+        n = 1;
+        w = 0.0f;
+    }
+    const float inv_n = 1.0f / (float)n;
+    const float sden = w * inv_n;
+    const float mag = __fsqrt_rn(dist2f(ex, ey, ez));
+    const float im = mag > 0.0f ? 1.0f / mag : 0.0f;
+    float p1, p2, p3;
+    langevin3(mag, p1, p2, p3);
+    const float third_n = inv_n * (1.0f / 3.0f);
+    a.out.pos_s[pg] = make_float4(px, py, pz, sden);
+    a.out.ehat[pg] = make_float4(ex * im, ey * im, ez * im, inv_n);
+    a.out.amp[pg] = make_float4(kP0 * p1 * sden, kQ0 * p2 * sden, kO0 * p3 * sden, 0.0f);
+    a.out.e0[pg] = make_float4(fx * third_n, fy * third_n, fz * third_n, 0.0f);
+}
+
+template <int MASK>
+__global__ void __launch_bounds__(kForceThreads) force_kernel(ForceArgs a) {
+    __shared__ float4 s_p[kForceThreads], s_eh[kForceThreads], s_am[kForceThreads], s_e0[kForceThreads];
+    const int4 item = a.items[blockIdx.x];
+    const WinDev W = a.win[item.x];
+    const int2 ch = a.chunks[item.w];
+    const int t = threadIdx.x;
+    const bool active = t < item.z;
+    const int ai = item.y + (active ? t : 0);
+    const float4 xi = a.pos[ai];
+    const int ity = a.atype[ai].y;
+    const float rm = __ldg(a.rmax + ity);
+    const float rm2 = __fmul_rn(rm, rm);
+    const int frow = ity * a.n_f;
+    const int terms = MASK >= 0 ? MASK : a.terms;
+    const float L = W.box, h = W.hbox;
+    const float f_r0 = a.f_r0, f_dr = a.f_dr, f_inv = a.f_inv;
+    const int nf = a.n_f;
+
+    float qx = 0.f, qy = 0.f, qz = 0.f;  // terms proportional to -q_i vtot_i
+    float lx = 0.f, ly = 0.f, lz = 0.f;  // tabulated LJ, proportional to -vtot_i
+
+    for (int p0 = 0; p0 < ch.y; p0 += kForceThreads) {
+        const int pn = min(kForceThreads, ch.y - p0);
+        __syncthreads();
+        if (t < pn) {
+            const long long pg = (long long)ch.x + p0 + t;
+            s_p[t] = a.pts.pos_s[pg];
+            s_eh[t] = a.pts.ehat[pg];
+            s_am[t] = a.pts.amp[pg];
+            s_e0[t] = a.pts.e0[pg];
+        }
+        __syncthreads();
+#pragma unroll 2
+        for (int k = 0; k < pn; ++k) {
+            const float4 P = s_p[k];
+            const float rx = mimg(P.x - xi.x, L, h);
+            const float ry = mimg(P.y - xi.y, L, h);
+            const float rz = mimg(P.z - xi.z, L, h);
+            const float d2 = dist2f(rx, ry, rz);
+            const float ri = rsqrtf(d2);
+            const float ri2 = ri * ri;
+            if (terms & 1) {  // dipole / quadrupole / octupole (:274-289)
+                const float4 E = s_eh[k];
+                const float4 A = s_am[k];
+                const float Rz = (E.x * rx + E.y * ry + E.z * rz) * ri;
+                const float Rz2 = Rz * Rz;
+                const float dp1 = 3.0f * Rz;
+                const float dp2 = fmaf(7.5f, Rz2, -1.5f);
+                const float dp3 = fmaf(17.5f, Rz2, -7.5f) * Rz;
+                const float t1 = A.x * ri2 * ri;
+                const float t2 = A.y * ri2 * ri2;
+                const float t3 = A.z * ri2 * ri2 * ri;
+                const float cR = fmaf(t1, dp1, fmaf(t2, dp2, t3 * dp3)) * ri;
+                const float cE = fmaf(t2, dp1, fmaf(t3, dp2, t1));
+                qx = fmaf(cR, rx, fmaf(-cE, E.x, qx));
+                qy = fmaf(cR, ry, fmaf(-cE, E.y, qy));
+                qz = fmaf(cR, rz, fmaf(-cE, E.z, qz));
+            }
+            if (d2 <= rm2) {
+                if (terms & 2) {  // tabulated mean LJ force (:291-305)
+                    const float dist = __fsqrt_rn(d2);
+                    const int bin = (int)__fmaf_rn(__fsub_rn(dist, f_r0), f_inv, 0.5f);
+                    if (bin >= 0 && bin < nf) {
+                        const float2 tv = __ldg(a.ftab + frow + bin);
+                        const float fr = (dist - fmaf((float)bin, f_dr, f_r0)) * f_inv;
+                        const float fv = fmaf(fr, tv.y - tv.x, tv.x) * P.w * ri;
+                        lx = fmaf(fv, rx, lx);
+                        ly = fmaf(fv, ry, ly);
+                        lz = fmaf(fv, rz, lz);
+                    }
+                }
+            } else if (terms & 4) {  // constant-density dielectric (:306-312)
+                const float4 E0 = s_e0[k];
+                const float tc = kP0 * ri2 * ri;
+                const float pd = 3.0f * (E0.x * rx + E0.y * ry + E0.z * rz) * ri2;
+                qx = fmaf(tc, fmaf(pd, rx, -E0.x), qx);
+                qy = fmaf(tc, fmaf(pd, ry, -E0.y), qy);
+                qz = fmaf(tc, fmaf(pd, rz, -E0.z), qz);
+            }
+        }
+    }
+    if (!active) return;
+    const float vt = __ldg(a.vtot + ity);
+    const float Fx = -vt * fmaf(xi.w, qx, lx);
+    const float Fy = -vt * fmaf(xi.w, qy, ly);
+    const float Fz = -vt * fmaf(xi.w, qz, lz);
+    check_force(a.status, Fx, Fy, Fz);
+    fix_add3(a.facc + 3 * (long long)ai, Fx, Fy, Fz);
+}
+
+template <int S, bool GEN, bool RAW>
+void launch_field_t(const FieldArgs &a, cudaStream_t s) {
+    field_kernel<S, GEN, RAW><<<a.n_tiles, kFieldThreads, 0, s>>>(a);
+}
+
+template <int S>
+void launch_field_s(const FieldArgs &a, bool raw, cudaStream_t s) {
+    const bool gen = a.pts_in == nullptr;
+    if (gen && !raw) launch_field_t<S, true, false>(a, s);
+    else if (gen && raw) launch_field_t<S, true, true>(a, s);
+    else if (!gen && !raw) launch_field_t<S, false, false>(a, s);
+    else launch_field_t<S, false, true>(a, s);
+}
+
+}  // namespace
+
+int field_block_threads() { return kFieldThreads; }
+int force_block_threads() { return kForceThreads; }
+
+void launch_field(const FieldArgs &a, int split, bool raw, cudaStream_t s) {
+    if (a.n_tiles <= 0) return;
+    if (split == 4) launch_field_s<4>(a, raw, s);
+    else if (split == 2) launch_field_s<2>(a, raw, s);
+    else launch_field_s<1>(a, raw, s);
+}
+
+void launch_force(const ForceArgs &a, cudaStream_t s) {
+    if (a.n_items <= 0) return;
+    if (a.terms == 7) force_kernel<7><<<a.n_items, kForceThreads, 0, s>>>(a);
+    else force_kernel<-1><<<a.n_items, kForceThreads, 0, s>>>(a);
+}
+
+}  // namespace isspa

@@ -1,0 +1,146 @@
+// kernels.h -- argument blocks and launch wrappers of the device kernels.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "device_common.cuh"
+
+namespace isspa {
+
+// ---- IS-SPA field pass (one thread-column per MC point) ------------------
+struct FieldArgs {
+    const float4 *pos;     // [Ntot] x, y, z, q
+    const int2 *atype;     // [Ntot] lj type, isspa type
+    const WinDev *win;
+    const int4 *tiles;     // [n_tiles] window, first point (global), n points, 0
+    int n_tiles;
+    const float4 *gtab;    // [n_itypes * n_gbins] g_b, g_b+1, e_b, e_b+1
+    const float *rmax;     // [n_itypes]
+    int n_gbins;           // nG - 1
+    float g_r0, g_dr, g_inv, e_r0, e_dr, e_inv;
+    float e0;
+    int n_mc;
+    uint32_t seed_lo, seed_hi;
+    const uint32_t *step_ptr;  // device step counter
+    const float *pts_in;   // injected points [P][3] (global order) or nullptr
+    PointsDev out;
+    float4 *raw_e;         // optional: E, w
+    float4 *raw_e0;        // optional: E0, n
+    int *status;
+};
+
+// ---- IS-SPA force pass (one thread per receiving atom) -------------------
+struct ForceArgs {
+    const float4 *pos;
+    const int2 *atype;
+    const WinDev *win;
+    const int4 *items;     // window, first atom (global), n atoms, chunk index
+    const int2 *chunks;    // [chunk index]: first point (global), n points
+    int n_items;
+    PointsDev pts;
+    const float2 *ftab;    // [n_itypes * n_f] packed (f_k, f_k+1), flat semantics
+    const float *rmax;
+    const float *vtot;
+    int n_f;
+    float f_r0, f_dr, f_inv;
+    int terms;             // 1 multipole, 2 tabulated LJ, 4 CDD
+    unsigned long long *facc;  // [Ntot][3]
+    int *status;
+};
+
+// ---- all-pairs nonbond --------------------------------------------------
+struct NonbondArgs {
+    const float4 *pos;
+    const int2 *atype;
+    const int *atom_win;       // [Ntot]
+    const WinDev *win;
+    const int4 *items;         // window, first i (global), n i, first j (global)
+    const int *items_nj;       // [n_items]
+    int n_items;
+    const float2 *ljab;        // [n_lj_types^2] A, B (expanded from nb_parm_index)
+    int n_lj_types;
+    const float *rmax;
+    const int *excl_start;     // [Ntot+1] CSR of symmetric exclusions (global, sorted)
+    const int *excl;
+    int terms;                 // 1 LJ, 2 Coulomb, 4 IS-SPA correction
+    unsigned long long *facc;
+    int *status;
+};
+
+// ---- bonded + umbrella ----------------------------------------------------
+struct BondedArgs {
+    const float4 *pos;
+    const int *atom_win;
+    const WinDev *win;
+    const int4 *bonds;         // i, j, type, -
+    int n_bonds;
+    const float2 *bond_par;    // 2k, r0
+    const int4 *angles;        // i, j, k, type
+    int n_angles;
+    const float2 *angle_par;
+    const int4 *dihs;          // i, j, +-k, +-l
+    const int *dih_type;
+    int n_dihs;
+    const float4 *dih_par;     // n, k, phase, -
+    const float2 *sc14;        // scee, scnb
+    const float2 *ljab;
+    const int2 *atype;
+    int n_lj_types;
+    int do_bonds, do_angles, do_dihs;
+    unsigned long long *facc;
+    int *status;
+};
+
+struct UmbrellaArgs {
+    const float4 *pos;
+    const WinDev *win;
+    const int *us_windows;     // windows with a restraint
+    int n_us_windows;
+    const int2 *bias;          // global atom, group
+    const float *mfrac;        // mass fraction within its group
+    double *com;               // [n_windows][2][3]
+    double *cv;                // [n_windows]
+    unsigned long long *facc;
+    int *status;
+};
+
+struct LeapfrogArgs {
+    float4 *pos;
+    float4 *vel;
+    float4 *force_out;         // converted forces of this step
+    unsigned long long *facc;  // read and cleared
+    const int *atom_win;
+    const WinDev *win;
+    int n_atoms;
+    uint32_t seed_lo, seed_hi;
+    uint32_t *step_ptr;        // advanced by the last block to finish
+    unsigned int *done_ptr;    // block-completion counter (self-resetting)
+    int *status;
+};
+
+struct ListArgs {
+    const float4 *pos;
+    const int *excl_start;
+    const int *excl;
+    int atom_off, n_atoms;
+    float box, hbox, rnn2;
+    int max_per_atom;
+    int *rows;                 // [n][max_per_atom]
+    int *counts;
+};
+
+void launch_field(const FieldArgs &a, int split, bool raw, cudaStream_t s);
+void launch_force(const ForceArgs &a, cudaStream_t s);
+void launch_nonbond(const NonbondArgs &a, cudaStream_t s);
+void launch_bonded(const BondedArgs &a, cudaStream_t s);
+void launch_umbrella(const UmbrellaArgs &a, cudaStream_t s);
+void launch_leapfrog(const LeapfrogArgs &a, cudaStream_t s);
+void launch_neighbor_list(const ListArgs &a, cudaStream_t s);
+void launch_cell_index(const float4 *pos, int atom_off, int n, float rc, int3 ncell, int *cell,
+                       cudaStream_t s);
+double measure_fp32_peak_tflops();
+int field_block_threads();
+int force_block_threads();
+int nonbond_block_threads();
+
+}  // namespace isspa

@@ -1,0 +1,201 @@
+"""Python handle on the GB300 engine (thin wrapper over the C ABI).
+
+Method names follow the reference's per-step wrappers (bond_force_cuda,
+isspa_force_cuda, ... in src/*_force_cuda.cu); each adds into the engine's
+force accumulator exactly as the reference kernels add into for_d.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Iterable, Optional, Sequence
+
+import numpy as np
+
+from . import abi
+from .system import System
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Engine:
+    def __init__(self, windows: "System | Sequence[System]", isspa_terms: int = 7,
+                 nonbond_terms: int = 7, use_graph: bool = True, field_split: int = 0,
+                 force_chunk: int = 0, mem_cap: int = 0):
+        if isinstance(windows, System):
+            windows = [windows]
+        self.windows = list(windows)
+        L = abi.lib()
+        descs = (abi.SystemDesc * len(self.windows))()
+        keep = []
+        for k, w in enumerate(self.windows):
+            d, kp = w.to_desc()
+            descs[k] = d
+            keep.append(kp)
+        opt = abi.EngineOptions()
+        L.isspa_default_options(C.byref(opt))
+        opt.isspa_terms, opt.nonbond_terms = int(isspa_terms), int(nonbond_terms)
+        opt.use_graph, opt.field_split, opt.force_chunk = int(use_graph), int(field_split), int(force_chunk)
+        opt.mem_cap = int(mem_cap)
+        h = C.c_void_p()
+        abi.check(L.isspa_engine_create(descs, len(self.windows), C.byref(opt), C.byref(h)), "engine create")
+        self._h = h
+        nw, na, npt = C.c_int(), C.c_int(), C.c_longlong()
+        L.isspa_engine_info(h, C.byref(nw), C.byref(na), C.byref(npt))
+        self.n_windows, self.n_atoms, self.n_points = nw.value, na.value, npt.value
+
+    # -------------------------------------------------------------- lifetime
+    def close(self):
+        if getattr(self, "_h", None):
+            abi.lib().isspa_engine_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -------------------------------------------------- per-step force calls
+    def _call(self, name: str, timed: bool):
+        ms = C.c_float(0.0)
+        fn = getattr(abi.lib(), name)
+        abi.check(fn(self._h, C.byref(ms) if timed else None), name)
+        return ms.value if timed else None
+
+    def zero_forces(self):
+        abi.check(abi.lib().isspa_zero_forces(self._h), "zero")
+
+    def bond_force(self, timed=False):
+        return self._call("bond_force_cuda", timed)
+
+    def angle_force(self, timed=False):
+        return self._call("angle_force_cuda", timed)
+
+    def dih_force(self, timed=False):
+        return self._call("dih_force_cuda", timed)
+
+    def isspa_force(self, timed=False):
+        return self._call("isspa_force_cuda", timed)
+
+    def nonbond_force(self, timed=False):
+        return self._call("nonbond_force_cuda", timed)
+
+    def us_force(self, timed=False):
+        return self._call("us_force_cuda", timed)
+
+    def leapfrog(self, timed=False):
+        return self._call("leapfrog_cuda", timed)
+
+    def compute_forces(self):
+        """All force terms of one step in the reference order (total_force_cuda.cpp:109-129)."""
+        self.zero_forces()
+        self.bond_force()
+        self.angle_force()
+        self.dih_force()
+        self.isspa_force()
+        self.nonbond_force()
+        self.us_force()
+        return self.forces()
+
+    def step(self, nsteps: int = 1):
+        abi.check(abi.lib().isspa_step(self._h, int(nsteps)), "step")
+
+    def time_steps(self, nsteps: int, flush_bytes: int = 0) -> float:
+        ms = C.c_double(0.0)
+        abi.check(abi.lib().isspa_time_steps(self._h, int(nsteps), int(flush_bytes), C.byref(ms)), "time")
+        return ms.value
+
+    def synchronize(self):
+        abi.check(abi.lib().isspa_synchronize(self._h), "synchronize")
+
+    def device_status(self, reset: bool = False) -> int:
+        return abi.lib().isspa_device_status(self._h, int(reset))
+
+    # ------------------------------------------------------------ state I/O
+    def _get4(self, name: str) -> np.ndarray:
+        out = np.zeros((self.n_atoms, 4), np.float32)
+        abi.check(getattr(abi.lib(), name)(self._h, _ptr(out), self.n_atoms), name)
+        return out
+
+    def positions(self):
+        return self._get4("isspa_get_positions")
+
+    def velocities(self):
+        return self._get4("isspa_get_velocities")
+
+    def forces(self) -> np.ndarray:
+        return self._get4("isspa_get_forces")[:, :3]
+
+    def set_positions(self, pos4):
+        a = np.ascontiguousarray(pos4, np.float32).reshape(self.n_atoms, 4)
+        abi.check(abi.lib().isspa_set_positions(self._h, _ptr(a), self.n_atoms), "set positions")
+
+    def set_velocities(self, vel4):
+        a = np.ascontiguousarray(vel4, np.float32).reshape(self.n_atoms, 4)
+        abi.check(abi.lib().isspa_set_velocities(self._h, _ptr(a), self.n_atoms), "set velocities")
+
+    def set_step(self, step: int):
+        abi.check(abi.lib().isspa_set_step(self._h, int(step)), "set step")
+
+    def get_step(self) -> int:
+        s = C.c_uint32()
+        abi.check(abi.lib().isspa_get_step(self._h, C.byref(s)), "get step")
+        return s.value
+
+    def us_com(self):
+        com = np.zeros((self.n_windows, 2, 3))
+        cv = np.zeros(self.n_windows)
+        abi.check(abi.lib().isspa_get_us_com(self._h, _ptr(com), _ptr(cv)), "us com")
+        return com, cv
+
+    def step_host(self, pos_in, vel_in, pos_out, vel_out, force_out):
+        args = [_ptr(a) if a is not None else None for a in (pos_in, vel_in, pos_out, vel_out, force_out)]
+        abi.check(abi.lib().isspa_step_host(self._h, *args), "step_host")
+
+    # ----------------------------------------------------------- MC points
+    def set_mc_points(self, xyz):
+        a = np.ascontiguousarray(xyz, np.float32).reshape(self.n_points, 3)
+        abi.check(abi.lib().isspa_set_mc_points(self._h, _ptr(a), self.n_points), "set points")
+
+    def clear_mc_points(self):
+        abi.check(abi.lib().isspa_clear_mc_points(self._h), "clear points")
+
+    def point_fields(self):
+        P = self.n_points
+        xyz = np.zeros((P, 3), np.float32)
+        w = np.zeros(P, np.float32)
+        n = np.zeros(P, np.int32)
+        E = np.zeros((P, 3), np.float32)
+        E0 = np.zeros((P, 3), np.float32)
+        abi.check(abi.lib().isspa_get_point_fields(self._h, _ptr(xyz), _ptr(w), _ptr(n), _ptr(E), _ptr(E0), P),
+                  "point fields")
+        return xyz, w, n, E, E0
+
+    # --------------------------------------------------------------- lists
+    def neighbor_list(self, rnn: float, max_per_atom: int = 576):
+        n = self.windows[0].n_atoms
+        rows = np.zeros((n, max_per_atom), np.int32)
+        counts = np.zeros(n, np.int32)
+        abi.check(abi.lib().isspa_neighbor_list(self._h, float(rnn), int(max_per_atom), _ptr(rows), _ptr(counts)),
+                  "neighbor list")
+        return rows, counts
+
+    def cell_list(self, rc: float, ncell: Iterable[int]):
+        nc = np.ascontiguousarray(list(ncell), np.int32)
+        cell = np.zeros(self.windows[0].n_atoms, np.int32)
+        abi.check(abi.lib().isspa_cell_list(self._h, float(rc), _ptr(nc), _ptr(cell)), "cell list")
+        return cell
+
+
+def measure_fp32_peak() -> float:
+    v = C.c_double()
+    abi.check(abi.lib().isspa_measure_fp32_peak(C.byref(v)), "fp32 peak")
+    return v.value

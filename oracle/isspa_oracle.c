@@ -1,0 +1,579 @@
+/*
+ * isspa_oracle.c -- CPU oracle (test infrastructure only; see isspa_oracle.h).
+ *
+ * Plain-C restatement of the reference kernels.  Each function cites the
+ * reference file:line it follows.  Built with -ffp-contract=off so that the
+ * float geometry below is evaluated exactly as written (explicit fmaf where the
+ * GPU kernels fuse), on x86-64 and aarch64 alike.
+ */
+#include "isspa_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* IS-SPA constants, src/constants.h:6-13 (float literals there). */
+#define ORC_EP 2.3473f
+#define ORC_RHO 0.0075f
+#define ORC_P0 4.173705894203977f
+#define ORC_Q0 1.6899960102882601f
+#define ORC_O0 9.3658298730779350f
+#define ORC_PI 3.1415926535f
+
+static double orc_e0(void) {
+    /* e0 = 3/(4*PI*rho*p0)*(1-1/ep), evaluated in float as the macro is. */
+    float e0 = 3.0f / (4.0f * ORC_PI * ORC_RHO * ORC_P0) * (1.0f - 1.0f / ORC_EP);
+    return (double)e0;
+}
+
+void orc_set_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
+
+/* ---------------------------------------------------------------------------
+ * Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy
+ * as 1, 2, 3", SC'11).  Pinned by the Random123 known-answer vectors in tests.
+ * ------------------------------------------------------------------------- */
+void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+    uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+    uint32_t k0 = key[0], k1 = key[1];
+    for (int r = 0; r < 10; ++r) {
+        if (r) {
+            k0 += 0x9E3779B9u;
+            k1 += 0xBB67AE85u;
+        }
+        uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+        uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+        uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0;
+        uint32_t n1 = (uint32_t)p1;
+        uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+        uint32_t n3 = (uint32_t)p0;
+        c0 = n0; c1 = n1; c2 = n2; c3 = n3;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+static inline float u24(uint32_t x) { return (float)(x >> 8) * 5.9604644775390625e-08f; }
+static inline double u24open(uint32_t x) { return ((double)(x >> 8) + 1.0) * 5.9604644775390625e-08; }
+
+/* Minimum image, at most one box away (cuda_vector_routines.h:28-47 of the
+ * reference, i.e. src/cuda_vector_routines.h min_image). */
+static inline float mimg(float r, float L, float h) {
+    if (r > h) return r - L;
+    if (r < -h) return r + L;
+    return r;
+}
+static inline float dist2f(float x, float y, float z) { return fmaf(z, z, fmaf(y, y, x * x)); }
+
+/* ---------------------------------------------------------------------------
+ * K1: MC points, src/isspa_force_cuda.cu:73-107.  Rejection-sampled uniform
+ * ball r^2 < 0.99 (:92-97), scaled by rmax of the owner's type and translated
+ * to the owner (:99-100).  The curand XORWOW stream is replaced by Philox keyed
+ * by (seed, step, window, point, attempt).
+ * ------------------------------------------------------------------------- */
+void orc_mc_points(const orc_isspa_sys *s, int n_mc, uint64_t seed, uint32_t step,
+                   uint32_t window, float *pts) {
+    const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    const long P = (long)s->n_atoms * n_mc;
+#pragma omp parallel for schedule(static)
+    for (long p = 0; p < P; ++p) {
+        int a = (int)(p / n_mc);
+        float rm = s->rmax[s->isspa_type[a]];
+        float mx = 0.f, my = 0.f, mz = 0.f;
+        int ok = 0;
+        for (uint32_t att = 0; att < 64u && !ok; ++att) {
+            uint32_t ctr[4] = {(uint32_t)p, att, step, (window << 8) | 0u}, o[4];
+            orc_philox4x32_10(ctr, key, o);
+            mx = fmaf(2.0f, u24(o[0]), -1.0f);
+            my = fmaf(2.0f, u24(o[1]), -1.0f);
+            mz = fmaf(2.0f, u24(o[2]), -1.0f);
+            ok = dist2f(mx, my, mz) < 0.99f;
+        }
+        if (!ok) { /* 64 rejections in a row (p ~ 1e-20): fixed offset, never the atom itself */
+            mx = 0.5f; my = mz = 0.f;
+        }
+        const float *xa = s->pos + 4 * a;
+        pts[3 * p + 0] = fmaf(mx, rm, xa[0]);
+        pts[3 * p + 1] = fmaf(my, rm, xa[1]);
+        pts[3 * p + 2] = fmaf(mz, rm, xa[2]);
+    }
+}
+
+/* ---------------------------------------------------------------------------
+ * K2: field, src/isspa_force_cuda.cu:110-206.  Per point p owned by atom a:
+ *   inside rmax[type(a)] (:154): count (:155); g lerped with the g-grid bin
+ *   (:157-167), bin<0 => density 0 (:159-160), bin>=nGRs-1 => factor 1;
+ *   mean field += r*etab/d with the same bin on the E-grid (:171-176);
+ *   outside: E0 -= e0*q*r/d^3 (:179);  always E -= e0*q*r/d^3 (:183).
+ * Flattened table rows: bin+1 may run into the next type's row as in the
+ * reference; the caller pads each table with zeros at its end.
+ * ------------------------------------------------------------------------- */
+void orc_field(const orc_isspa_sys *s, int n_mc, const float *pts, double *w, int *cnt,
+               double *efield, double *e0field) {
+    const int N = s->n_atoms;
+    const long P = (long)N * n_mc;
+    const float L = s->box, h = 0.5f * s->box;
+    const double e0 = orc_e0();
+    const float g_inv = 1.0f / s->g_dr;
+#pragma omp parallel for schedule(dynamic, 64)
+    for (long p = 0; p < P; ++p) {
+        const int a = (int)(p / n_mc);
+        const float rm = s->rmax[s->isspa_type[a]];
+        const float rm2 = rm * rm;
+        const float px = pts[3 * p], py = pts[3 * p + 1], pz = pts[3 * p + 2];
+        double wp = 1.0, E[3] = {0, 0, 0}, E0[3] = {0, 0, 0};
+        int n = 0;
+        for (int j = 0; j < N; ++j) {
+            const float *xj = s->pos + 4 * j;
+            const float rx = mimg(px - xj[0], L, h);
+            const float ry = mimg(py - xj[1], L, h);
+            const float rz = mimg(pz - xj[2], L, h);
+            const float d2 = dist2f(rx, ry, rz);
+            const double dx = rx, dy = ry, dz = rz;
+            const double dd = sqrt(dx * dx + dy * dy + dz * dz);
+            const double c = e0 * (double)xj[3] / (dd * dd * dd);
+            E[0] -= c * dx; E[1] -= c * dy; E[2] -= c * dz;
+            if (d2 <= rm2) {
+                ++n;
+                const float dist = sqrtf(d2);
+                const int bin = (int)((dist - s->g_r0) * g_inv);
+                const int jt = s->isspa_type[j];
+                if (bin < 0) {
+                    wp = 0.0;
+                } else if (bin < s->n_g - 1) {
+                    double fr = (dd - ((double)s->g_r0 + bin * (double)s->g_dr)) / s->g_dr;
+                    long gi = (long)jt * s->n_g + bin;
+                    wp *= s->g_table[gi] * (1.0 - fr) + s->g_table[gi + 1] * fr;
+                    double fe = (dd - ((double)s->e_r0 + bin * (double)s->e_dr)) / s->e_dr;
+                    long ei = (long)jt * s->n_e + bin;
+                    double et = s->e_table[ei] * (1.0 - fe) + s->e_table[ei + 1] * fe;
+                    E[0] += dx * et / dd; E[1] += dy * et / dd; E[2] += dz * et / dd;
+                }
+            } else {
+                E0[0] -= c * dx; E0[1] -= c * dy; E0[2] -= c * dz;
+            }
+        }
+        w[p] = wp;
+        cnt[p] = n;
+        for (int k = 0; k < 3; ++k) {
+            efield[3 * p + k] = E[k];
+            e0field[3 * p + k] = E0[k];
+        }
+    }
+}
+
+/* Langevin averages for a dipole in field x: <P1>=coth x-1/x (c1 of
+ * isspa_force_cuda.cu:271), <P2>=1.5*c2-0.5 (:283), <P3>=2.5*c3-1.5*c1 (:287).
+ * The closed forms cancel catastrophically as x->0; below 0.25 the Taylor
+ * series of the same functions is used. */
+void orc_langevin(double x, double out[3]) {
+    if (x < 0.25) {
+        const double x2 = x * x;
+        static const double a1[] = {1.0 / 3, -1.0 / 45, 2.0 / 945, -1.0 / 4725, 2.0 / 93555,
+                                    -1382.0 / 638512875, 4.0 / 18243225};
+        static const double a2[] = {1.0 / 15, -2.0 / 315, 1.0 / 1575, -2.0 / 31185,
+                                    1382.0 / 212837625, -4.0 / 6081075};
+        static const double a3[] = {1.0 / 105, -1.0 / 945, 17.0 / 155925, -472.0 / 42567525,
+                                    718.0 / 638512875, -1237.0 / 10854718875.0};
+        double s1 = 0, s2 = 0, s3 = 0;
+        for (int k = 6; k >= 0; --k) s1 = s1 * x2 + a1[k];
+        for (int k = 5; k >= 0; --k) s2 = s2 * x2 + a2[k];
+        for (int k = 5; k >= 0; --k) s3 = s3 * x2 + a3[k];
+        out[0] = x * s1;
+        out[1] = x2 * s2;
+        out[2] = x2 * x * s3;
+        return;
+    }
+    const double coth = 1.0 / tanh(x);
+    const double c1 = coth - 1.0 / x;
+    const double c2 = 1.0 - 2.0 * c1 / x;
+    const double c3 = coth - 3.0 * c2 / x;
+    out[0] = c1;
+    out[1] = 1.5 * c2 - 0.5;
+    out[2] = 2.5 * c3 - 1.5 * c1;
+}
+
+/* ---------------------------------------------------------------------------
+ * K3: force, src/isspa_force_cuda.cu:208-327.  For atom i and every point p:
+ *   rho = w_p * vtot[type i] / n_p (:253-254); unit field and |E| (:256-260);
+ *   E0/3 (:261-263); multipole force (:270-289); inside rmax[type i]: tabulated
+ *   mean LJ force with nearest-bin index and lerp (:291-305), bin>=nRs => 0
+ *   (:293-294); outside: constant-density dielectric (:306-312).
+ * A zero field (|E| == 0) contributes no multipole force (the reference
+ * divides 0/0 there).
+ * ------------------------------------------------------------------------- */
+void orc_isspa_force(const orc_isspa_sys *s, int n_mc, const float *pts, const double *w,
+                     const int *cnt, const double *efield, const double *e0field,
+                     int term_mask, double *f) {
+    const int N = s->n_atoms;
+    const long P = (long)N * n_mc;
+    const float L = s->box, h = 0.5f * s->box;
+    const float f_inv = 1.0f / s->f_dr;
+    const double p0 = ORC_P0, q0 = ORC_Q0, o0 = ORC_O0;
+    /* per-point prologue, computed once per point */
+    double *pp = (double *)malloc(sizeof(double) * 12 * (size_t)(P > 0 ? P : 1));
+#pragma omp parallel for schedule(static)
+    for (long p = 0; p < P; ++p) {
+        double *q = pp + 12 * p;
+        const double *E = efield + 3 * p;
+        const double mag = sqrt(E[0] * E[0] + E[1] * E[1] + E[2] * E[2]);
+        double lg[3];
+        orc_langevin(mag, lg);
+        const double inv_n = 1.0 / cnt[p];
+        q[0] = w[p] * inv_n; /* density per unit vtot */
+        q[1] = inv_n;
+        if (mag > 0) {
+            q[2] = E[0] / mag; q[3] = E[1] / mag; q[4] = E[2] / mag;
+        } else {
+            q[2] = q[3] = q[4] = 0.0;
+        }
+        q[5] = lg[0]; q[6] = lg[1]; q[7] = lg[2];
+        q[8] = e0field[3 * p] / 3.0; q[9] = e0field[3 * p + 1] / 3.0; q[10] = e0field[3 * p + 2] / 3.0;
+    }
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int i = 0; i < N; ++i) {
+        const float *xi = s->pos + 4 * i;
+        const int it = s->isspa_type[i];
+        const float rm = s->rmax[it];
+        const float rm2 = rm * rm;
+        const double vt = s->vtot[it];
+        const double qi = xi[3];
+        double F[3] = {0, 0, 0};
+        for (long p = 0; p < P; ++p) {
+            const double *q = pp + 12 * p;
+            const float rx = mimg(pts[3 * p] - xi[0], L, h);
+            const float ry = mimg(pts[3 * p + 1] - xi[1], L, h);
+            const float rz = mimg(pts[3 * p + 2] - xi[2], L, h);
+            const float d2 = dist2f(rx, ry, rz);
+            const double dx = rx, dy = ry, dz = rz;
+            const double dd2 = dx * dx + dy * dy + dz * dz;
+            const double dd = sqrt(dd2);
+            const double rho = q[0] * vt;
+            if (term_mask & ORC_ISSPA_MULTIPOLE) {
+                const double ex = q[2], ey = q[3], ez = q[4];
+                const double Rz = (ex * dx + ey * dy + ez * dz) / dd;
+                const double dp1 = 3.0 * Rz;
+                const double dp2 = 7.5 * Rz * Rz - 1.5;
+                const double dp3 = (17.5 * Rz * Rz - 7.5) * Rz;
+                double fs = -qi * p0 * q[5] * rho / (dd2 * dd);
+                F[0] += fs * (dx * dp1 / dd - ex);
+                F[1] += fs * (dy * dp1 / dd - ey);
+                F[2] += fs * (dz * dp1 / dd - ez);
+                fs = -qi * q0 * q[6] * rho / (dd2 * dd2);
+                F[0] += fs * (dx * dp2 / dd - dp1 * ex);
+                F[1] += fs * (dy * dp2 / dd - dp1 * ey);
+                F[2] += fs * (dz * dp2 / dd - dp1 * ez);
+                fs = -qi * o0 * q[7] * rho / (dd2 * dd2 * dd);
+                F[0] += fs * (dx * dp3 / dd - dp2 * ex);
+                F[1] += fs * (dy * dp3 / dd - dp2 * ey);
+                F[2] += fs * (dz * dp3 / dd - dp2 * ez);
+            }
+            if (d2 <= rm2) {
+                if (term_mask & ORC_ISSPA_LJ) {
+                    const float dist = sqrtf(d2);
+                    const int bin = (int)fmaf(dist - s->f_r0, f_inv, 0.5f);
+                    double fs = 0.0;
+                    if (bin >= 0 && bin < s->n_f) {
+                        const double fr = (dd - ((double)s->f_r0 + bin * (double)s->f_dr)) / s->f_dr;
+                        const long fi = (long)it * s->n_f + bin;
+                        fs = (s->f_table[fi] * (1.0 - fr) + s->f_table[fi + 1] * fr) * rho;
+                    }
+                    F[0] -= dx * fs / dd; F[1] -= dy * fs / dd; F[2] -= dz * fs / dd;
+                }
+            } else if (term_mask & ORC_ISSPA_CDD) {
+                const double igo = vt * q[1];
+                const double fs = -qi * p0 / (dd2 * dd);
+                const double pdr = 3.0 * (q[8] * dx + q[9] * dy + q[10] * dz) / dd2;
+                F[0] += fs * (pdr * dx - q[8]) * igo;
+                F[1] += fs * (pdr * dy - q[9]) * igo;
+                F[2] += fs * (pdr * dz - q[10]) * igo;
+            }
+        }
+        f[3 * i] += F[0]; f[3 * i + 1] += F[1]; f[3 * i + 2] += F[2];
+    }
+    free(pp);
+}
+
+/* Exclusion test with the reference's ascending-list scan semantics
+ * (nonbond_force_cuda.cu:72-108): the lower-index atom's list is walked in
+ * order and the scan stops at the first entry larger than the partner. */
+static int orc_excluded(const orc_nb_sys *s, int i, int j) {
+    int a = i < j ? i : j, b = i < j ? j : i;
+    if (a == b) return 0;
+    int start = a == 0 ? 0 : s->n_excl_cum[a - 1];
+    int stop = s->n_excl_cum[a];
+    for (int e = start; e < stop; ++e) {
+        if (s->excl_list[e] == b) return 1;
+        if (s->excl_list[e] > b) return 0;
+    }
+    return 0;
+}
+
+/* ---------------------------------------------------------------------------
+ * K4: nonbond, src/nonbond_force_cuda.cu:31-174.  Non-excluded pairs: LJ
+ * r^-6(12A r^-6 - 6B)/r^2 (:131-132) + Coulomb q1q2/r^3 (:136) + correction;
+ * excluded pairs: correction only (:153-162).  Correction (:141-147): r >
+ * 2 rmax[type j] => -2q1q2(1-1/ep)/(3r^3), else -q1q2(1-1/ep)(8rmax-3r)/(24
+ * rmax^4).  Force on atom i only.
+ * ------------------------------------------------------------------------- */
+void orc_nonbond(const orc_nb_sys *s, int term_mask, double *f) {
+    const int N = s->n_atoms;
+    const float L = s->box, h = 0.5f * s->box;
+    const double epf = 1.0 - 1.0 / (double)ORC_EP;
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int i = 0; i < N; ++i) {
+        const float *xi = s->pos + 4 * i;
+        double F[3] = {0, 0, 0};
+        for (int j = 0; j < N; ++j) {
+            if (j == i) continue;
+            const float *xj = s->pos + 4 * j;
+            const float rx = mimg(xi[0] - xj[0], L, h);
+            const float ry = mimg(xi[1] - xj[1], L, h);
+            const float rz = mimg(xi[2] - xj[2], L, h);
+            const float d2 = dist2f(rx, ry, rz);
+            const double dx = rx, dy = ry, dz = rz;
+            const double dd2 = dx * dx + dy * dy + dz * dz;
+            const double dd = sqrt(dd2);
+            const double qq = (double)xi[3] * (double)xj[3];
+            const float rmj = s->rmax[s->isspa_type[j]];
+            const float two = 2.0f * rmj;
+            double fs = 0.0;
+            if (term_mask & ORC_NB_CORR) {
+                if (d2 > two * two) {
+                    fs += -2.0 * qq * epf / (3.0 * dd2 * dd);
+                } else {
+                    const double r4 = (double)rmj * rmj * rmj * rmj;
+                    fs += -qq * epf * (8.0 * rmj - 3.0 * dd) / (24.0 * r4);
+                }
+            }
+            if (!orc_excluded(s, i, j)) {
+                if (term_mask & ORC_NB_LJ) {
+                    const int nlj = s->nb_parm_index[s->n_types * s->lj_type[i] + s->lj_type[j]];
+                    const double A = s->lj_ab[2 * nlj], B = s->lj_ab[2 * nlj + 1];
+                    const double r6 = 1.0 / (dd2 * dd2 * dd2);
+                    fs += r6 * (12.0 * A * r6 - 6.0 * B) / dd2;
+                }
+                if (term_mask & ORC_NB_COUL) fs += qq / (dd2 * dd);
+            }
+            F[0] += fs * dx; F[1] += fs * dy; F[2] += fs * dz;
+        }
+        f[3 * i] += F[0]; f[3 * i + 1] += F[1]; f[3 * i + 2] += F[2];
+    }
+}
+
+static inline void rvec(const float *pos, int a, int b, float L, float h, double r[3]) {
+    r[0] = mimg(pos[4 * a] - pos[4 * b], L, h);
+    r[1] = mimg(pos[4 * a + 1] - pos[4 * b + 1], L, h);
+    r[2] = mimg(pos[4 * a + 2] - pos[4 * b + 2], L, h);
+}
+
+/* K5: bond, src/bond_force_cuda.cu:36-50: f = 2k(r0/|r| - 1) r on atom x. */
+void orc_bonds(int nb, const int *atoms, const float *params, const float *pos, float box,
+               double *f) {
+    const float L = box, h = 0.5f * box;
+    for (int b = 0; b < nb; ++b) {
+        int x = atoms[3 * b], y = atoms[3 * b + 1], t = atoms[3 * b + 2];
+        double r[3];
+        rvec(pos, x, y, L, h, r);
+        double d = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+        double fb = params[2 * t] * (params[2 * t + 1] / d - 1.0);
+        for (int k = 0; k < 3; ++k) {
+            f[3 * x + k] += fb * r[k];
+            f[3 * y + k] -= fb * r[k];
+        }
+    }
+}
+
+/* K6: angle, src/angle_force_cuda.cu:19-52. */
+void orc_angles(int na, const int *atoms, const float *params, const float *pos, float box,
+                double *f) {
+    const float L = box, h = 0.5f * box;
+    for (int a = 0; a < na; ++a) {
+        int x = atoms[4 * a], y = atoms[4 * a + 1], z = atoms[4 * a + 2], t = atoms[4 * a + 3];
+        double r1[3], r2[3];
+        rvec(pos, x, y, L, h, r1);
+        rvec(pos, y, z, L, h, r2);
+        double c11 = r1[0] * r1[0] + r1[1] * r1[1] + r1[2] * r1[2];
+        double c22 = r2[0] * r2[0] + r2[1] * r2[1] + r2[2] * r2[2];
+        double c12 = r1[0] * r2[0] + r1[1] * r2[1] + r1[2] * r2[2];
+        double b = -c12 / sqrt(c11 * c22);
+        double theta = b >= 1.0 ? 1.0e-16 : (b <= -1.0 ? (double)ORC_PI : acos(b));
+        double fa = params[2 * t] * (theta - params[2 * t + 1]) / sqrt(c11 * c22 - c12 * c12);
+        for (int k = 0; k < 3; ++k) {
+            f[3 * x + k] += fa * (c12 / c11 * r1[k] - r2[k]);
+            f[3 * y + k] += fa * ((1.0 + c12 / c22) * r2[k] - (1.0 + c12 / c11) * r1[k]);
+            f[3 * z + k] += fa * (r1[k] - c12 / c22 * r2[k]);
+        }
+    }
+}
+
+/* K7: dihedral + scaled 1-4, src/dih_force_cuda.cu:48-135. */
+void orc_dihedrals(int nd, const int *atoms, const int *types, const float *params,
+                   const float *scaled14, const int *lj_type, const int *nb_parm_index,
+                   int n_types, const float *lj_ab, const float *pos, float box,
+                   int with_14, double *f) {
+    const float L = box, h = 0.5f * box;
+    for (int d = 0; d < nd; ++d) {
+        int ax = atoms[4 * d], ay = atoms[4 * d + 1], az = atoms[4 * d + 2], aw = atoms[4 * d + 3];
+        int t = types[d];
+        if (with_14 && az > 0 && aw > 0) { /* :60 */
+            int nlj = nb_parm_index[n_types * lj_type[ax] + lj_type[aw]];
+            double A = lj_ab[2 * nlj], B = lj_ab[2 * nlj + 1];
+            double r14[3];
+            rvec(pos, ax, aw, L, h, r14);
+            double rm = r14[0] * r14[0] + r14[1] * r14[1] + r14[2] * r14[2];
+            double r6 = 1.0 / (rm * rm * rm);
+            double fe = (double)pos[4 * ax + 3] * pos[4 * aw + 3] / (rm * sqrt(rm) * scaled14[2 * t]);
+            double fv = r6 * (12.0 * A * r6 - 6.0 * B) / (scaled14[2 * t + 1] * rm);
+            for (int k = 0; k < 3; ++k) {
+                f[3 * ax + k] += (fe + fv) * r14[k];
+                f[3 * aw + k] -= (fe + fv) * r14[k];
+            }
+        }
+        if (aw < 0) aw = -aw;
+        if (az < 0) az = -az;
+        double r12[3], r23[3], r34[3];
+        rvec(pos, ax, ay, L, h, r12);
+        rvec(pos, ay, az, L, h, r23);
+        rvec(pos, az, aw, L, h, r34);
+        double c11 = r12[0] * r12[0] + r12[1] * r12[1] + r12[2] * r12[2];
+        double c22 = r23[0] * r23[0] + r23[1] * r23[1] + r23[2] * r23[2];
+        double c12 = r12[0] * r23[0] + r12[1] * r23[1] + r12[2] * r23[2];
+        double c33 = r34[0] * r34[0] + r34[1] * r34[1] + r34[2] * r34[2];
+        double c23 = r23[0] * r34[0] + r23[1] * r34[1] + r23[2] * r34[2];
+        double c13 = r12[0] * r34[0] + r12[1] * r34[1] + r12[2] * r34[2];
+        double t1 = c13 * c22 - c12 * c23;
+        double t2 = c11 * c23 - c12 * c13;
+        double t3 = c12 * c12 - c11 * c22;
+        double t4 = c22 * c33 - c23 * c23;
+        double t5 = c13 * c23 - c12 * c33;
+        double t6 = -t1;
+        double b = sqrt(-t3 * t4);
+        double a = t6 / b;
+        double fd = 0.0;
+        if (a > -1.0 && a < 1.0) {
+            double phi = acos(a);
+            const float *pr = params + 4 * t;
+            fd = pr[0] * pr[1] * sin(pr[0] * phi - pr[2]) * c22 / (sin(phi) * b);
+        }
+        for (int k = 0; k < 3; ++k) {
+            double f1 = fd / t3 * (t1 * r12[k] + t2 * r23[k] + t3 * r34[k]);
+            double f4 = -fd / t4 * (t4 * r12[k] + t5 * r23[k] + t6 * r34[k]);
+            f[3 * ax + k] += f1;
+            f[3 * ay + k] += -(1.0 + c12 / c22) * f1 + c23 / c22 * f4;
+            f[3 * az + k] += c12 / c22 * f1 - (1.0 + c23 / c22) * f4;
+            f[3 * aw + k] += f4;
+        }
+    }
+}
+
+/* K9: umbrella, src/us_force_cuda.cu:14-48 with kumb = [-k, +k]
+ * (us_class.cpp:153-154).  COM from wrapped positions, mass fractions. */
+void orc_us(int nbias, const int *list, const float *mfrac, double k, double x0,
+            const float *pos, float box, double *f, double *com) {
+    double c[2][3] = {{0, 0, 0}, {0, 0, 0}};
+    for (int b = 0; b < nbias; ++b) {
+        int a = list[2 * b], g = list[2 * b + 1];
+        for (int d = 0; d < 3; ++d) c[g][d] += (double)mfrac[b] * pos[4 * a + d];
+    }
+    double L = box, h = 0.5 * box, r[3];
+    for (int d = 0; d < 3; ++d) {
+        r[d] = c[0][d] - c[1][d];
+        if (r[d] > h) r[d] -= L;
+        else if (r[d] < -h) r[d] += L;
+    }
+    double dist = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+    for (int b = 0; b < nbias; ++b) {
+        int a = list[2 * b], g = list[2 * b + 1];
+        double ku = g == 0 ? -k : k;
+        double pf = ku * (dist - x0) * mfrac[b] / dist;
+        for (int d = 0; d < 3; ++d) f[3 * a + d] += pf * r[d];
+    }
+    if (com)
+        for (int g = 0; g < 2; ++g)
+            for (int d = 0; d < 3; ++d) com[3 * g + d] = c[g][d];
+}
+
+/* K8: leapfrog + Andersen, src/leapfrog_cuda.cu:44-64.  Random numbers come
+ * from Philox stream 1 keyed by (seed, step, window, atom). */
+void orc_leapfrog(int n, const float *pos, const float *vel, const double *f, float kT,
+                  float dt, float pnu, float box, uint64_t seed, uint32_t step,
+                  uint32_t window, double *pos_out, double *vel_out, int *resampled) {
+    const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    for (int i = 0; i < n; ++i) {
+        uint32_t c0[4] = {(uint32_t)i, 0u, step, (window << 8) | 1u}, o0[4];
+        orc_philox4x32_10(c0, key, o0);
+        const float u = u24(o0[0]);
+        const double m = vel[4 * i + 3];
+        double v[3], x[3];
+        int res = u < pnu;
+        if (res) {
+            uint32_t c1[4] = {(uint32_t)i, 1u, step, (window << 8) | 1u}, o1[4];
+            orc_philox4x32_10(c1, key, o1);
+            const double twopi = 6.283185307179586;
+            double ra = sqrt(-2.0 * log(u24open(o1[0]))), rb = sqrt(-2.0 * log(u24open(o1[2])));
+            double nrm[3] = {ra * cos(twopi * u24open(o1[1])), ra * sin(twopi * u24open(o1[1])),
+                             rb * cos(twopi * u24open(o1[3]))};
+            double sd = sqrt((double)kT / m);
+            for (int d = 0; d < 3; ++d) v[d] = nrm[d] * sd + f[3 * i + d] * dt / (2.0 * m);
+        } else {
+            for (int d = 0; d < 3; ++d) v[d] = vel[4 * i + d] + f[3 * i + d] * dt / m;
+        }
+        for (int d = 0; d < 3; ++d) {
+            x[d] = pos[4 * i + d] + v[d] * dt;
+            if (x[d] > box) x[d] -= box;
+            else if (x[d] < 0.0) x[d] += box;
+            pos_out[3 * i + d] = x[d];
+            vel_out[3 * i + d] = v[d];
+        }
+        if (resampled) resampled[i] = res;
+    }
+}
+
+static int cmp_int(const void *a, const void *b) {
+    int x = *(const int *)a, y = *(const int *)b;
+    return (x > y) - (x < y);
+}
+
+/* K10: neighbour list, src/neighborlist_cuda.cu:37-96: every ordered pair
+ * atom1 != atom2, not excluded, with r^2 < rNN^2.  The reference appends in
+ * atomic order; the oracle returns each row sorted. */
+long orc_neighbor_list(const orc_nb_sys *s, float rnn2, int max_per_atom, int *rows,
+                       int *counts) {
+    const int N = s->n_atoms;
+    const float L = s->box, h = 0.5f * s->box;
+    long total = 0;
+    for (int i = 0; i < N; ++i) {
+        int c = 0;
+        for (int j = 0; j < N; ++j) {
+            if (j == i || orc_excluded(s, i, j)) continue;
+            const float *xi = s->pos + 4 * i, *xj = s->pos + 4 * j;
+            float rx = mimg(xi[0] - xj[0], L, h), ry = mimg(xi[1] - xj[1], L, h),
+                  rz = mimg(xi[2] - xj[2], L, h);
+            if (dist2f(rx, ry, rz) < rnn2) {
+                if (c < max_per_atom) rows[(long)i * max_per_atom + c] = j;
+                ++c;
+            }
+        }
+        int m = c < max_per_atom ? c : max_per_atom;
+        qsort(rows + (long)i * max_per_atom, (size_t)m, sizeof(int), cmp_int);
+        counts[i] = c;
+        total += c;
+    }
+    return total;
+}
+
+/* K11: cell index, src/cell_list_cuda.cu:27-29. */
+void orc_cell_index(int n, const float *pos, float rc, const int ncell[3], int *cell) {
+    for (int i = 0; i < n; ++i) {
+        int cx = (int)(pos[4 * i] / rc), cy = (int)(pos[4 * i + 1] / rc), cz = (int)(pos[4 * i + 2] / rc);
+        cell[i] = cx * ncell[1] * ncell[2] + cy * ncell[2] + cz;
+    }
+}

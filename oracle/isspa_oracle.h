@@ -1,0 +1,126 @@
+/*
+ * isspa_oracle.h -- CPU oracle for the IS-SPA force/step path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the reference
+ * CUDA kernels of mccullaghlab/ISSPA-Force-Cuda (src/isspa_force_cuda.cu,
+ * src/nonbond_force_cuda.cu, src/bond_force_cuda.cu, src/angle_force_cuda.cu,
+ * src/dih_force_cuda.cu, src/leapfrog_cuda.cu, src/us_force_cuda.cu) used as
+ * the checker for the GPU engine.  Only tests, the smoke check and the CPU
+ * baseline of bench.py may load it; the product never links it.
+ *
+ * Numerics: every value is accumulated in double.  Every geometric
+ * *decision* (minimum image, inside-rmax tests, table bin indices, the MC
+ * rejection test) is evaluated in float with the exact operation sequence the
+ * GPU kernels use (explicit fmaf, no contraction), so the oracle and the GPU
+ * take identical branches and only rounding of values differs.
+ *
+ * Parity pins: the nonbond sub-terms are pinned to the reference's FP64 golden
+ * force files (timing_tests/ADI2/10000MC/compare/ADI2.multi.frc.{LJsolu,Csolu,
+ * Csolv_pair}.dat); the IS-SPA force branches are pinned statistically to the
+ * reference's 1000-seed per-term frame averages (ISSPA_force_{LJsolv,Csolv,
+ * Csolv_CDD}_10000.xyz); the Philox generator is pinned to the published
+ * Random123 known-answer vectors.
+ */
+#ifndef ISSPA_ORACLE_H
+#define ISSPA_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* IS-SPA solvent model inputs of one system (isspa_class.h:10-67). */
+typedef struct {
+    int n_atoms;
+    const float *pos;        /* [n_atoms][4]: x, y, z, charge/sqrt(eps) */
+    const int *isspa_type;   /* [n_atoms], 0-based */
+    int n_itypes;
+    const float *rmax;       /* [n_itypes] */
+    const float *vtot;       /* [n_itypes], isspa_class.cpp:41 */
+    int n_g, n_e, n_f;       /* rows per type of the three tables */
+    const float *g_table;    /* [n_itypes*n_g] (+ zero padding, see below) */
+    const float *e_table;    /* [n_itypes*n_e] */
+    const float *f_table;    /* [n_itypes*n_f] */
+    float g_r0, g_dr, e_r0, e_dr, f_r0, f_dr;
+    float box;
+} orc_isspa_sys;
+
+/* Nonbond inputs (atom_class.h:22-49). */
+typedef struct {
+    int n_atoms;
+    const float *pos;          /* [n_atoms][4] */
+    int n_types;
+    const int *lj_type;        /* [n_atoms] 0-based */
+    const int *nb_parm_index;  /* [n_types*n_types] 0-based index into lj_ab */
+    const float *lj_ab;        /* [n_types*(n_types+1)/2][2] A, B */
+    const int *n_excl_cum;     /* [n_atoms] cumulative counts */
+    const int *excl_list;      /* [excl_len] 0-based */
+    const int *isspa_type;     /* [n_atoms] */
+    const float *rmax;         /* [n_itypes] */
+    float box;
+} orc_nb_sys;
+
+/* Term masks, naming follows the reference's per-term golden files. */
+enum {
+    ORC_ISSPA_MULTIPOLE = 1, /* "Csolv": dipole+quadrupole+octupole polarisation */
+    ORC_ISSPA_LJ = 2,        /* "LJsolv": tabulated mean LJ force           */
+    ORC_ISSPA_CDD = 4,       /* "Csolv_CDD": constant-density dielectric    */
+    ORC_NB_LJ = 1,           /* "LJsolu" */
+    ORC_NB_COUL = 2,         /* "Csolu" */
+    ORC_NB_CORR = 4          /* "Csolv_pair": IS-SPA long-range correction  */
+};
+
+void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+
+/* MC points of one step (isspa_force_cuda.cu:73-107, Philox-keyed). */
+void orc_mc_points(const orc_isspa_sys *s, int n_mc, uint64_t seed, uint32_t step,
+                   uint32_t window, float *pts /* [N*n_mc][3] */);
+
+/* Density product, count and mean fields per MC point (isspa_force_cuda.cu:110-206). */
+void orc_field(const orc_isspa_sys *s, int n_mc, const float *pts, double *w, int *cnt,
+               double *efield /* [P][3] */, double *e0field /* [P][3] */);
+
+/* IS-SPA force on every atom from every MC point (isspa_force_cuda.cu:208-327). */
+void orc_isspa_force(const orc_isspa_sys *s, int n_mc, const float *pts, const double *w,
+                     const int *cnt, const double *efield, const double *e0field,
+                     int term_mask, double *f /* [N][3], accumulated into */);
+
+/* Langevin polarisation averages <P1>, <P2>, <P3> for field magnitude x. */
+void orc_langevin(double x, double out[3]);
+
+/* All-pairs LJ + Coulomb + IS-SPA correction (nonbond_force_cuda.cu:31-174). */
+void orc_nonbond(const orc_nb_sys *s, int term_mask, double *f /* [N][3] += */);
+
+/* Bonded terms (bond_force_cuda.cu:15-53, angle_force_cuda.cu:12-66, dih_force_cuda.cu:13-136). */
+void orc_bonds(int nb, const int *atoms, const float *params, const float *pos, float box, double *f);
+void orc_angles(int na, const int *atoms, const float *params, const float *pos, float box, double *f);
+void orc_dihedrals(int nd, const int *atoms, const int *types, const float *params,
+                   const float *scaled14, const int *lj_type, const int *nb_parm_index,
+                   int n_types, const float *lj_ab, const float *pos, float box,
+                   int with_14, double *f);
+
+/* Umbrella COM restraint (us_force_cuda.cu:14-48); com_out[2][3]. */
+void orc_us(int nbias, const int *list, const float *mfrac, double k, double x0,
+            const float *pos, float box, double *f, double *com_out);
+
+/* Leapfrog + Andersen (leapfrog_cuda.cu:33-68).  Reads float pos/vel, writes
+ * double results. */
+void orc_leapfrog(int n, const float *pos, const float *vel, const double *f, float kT,
+                  float dt, float pnu, float box, uint64_t seed, uint32_t step,
+                  uint32_t window, double *pos_out, double *vel_out, int *resampled);
+
+/* Neighbour list rows (neighborlist_cuda.cu:11-137): per-atom sorted partners
+ * with r^2 < rnn2, exclusions as the nonbond kernel.  Returns total count;
+ * rows[atom*max_per_atom + k], counts[atom]. */
+long orc_neighbor_list(const orc_nb_sys *s, float rnn2, int max_per_atom, int *rows,
+                       int *counts);
+
+/* Cell binning (cell_list_cuda.cu:13-35). cell[atom]. */
+void orc_cell_index(int n, const float *pos, float rc, const int ncell[3], int *cell);
+
+void orc_set_threads(int n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
