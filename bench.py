@@ -1,0 +1,337 @@
+"""Benchmark: IS-SPA MD throughput (atom-steps/s, ns/day) on one GB300.
+
+Workload: the plain drop-in path on the 1100-atom system (50 chains of 22
+atoms, nMC = 50, 60 A box, all-pairs FP32 nonbond + IS-SPA, Andersen at
+298 K), synthetic inputs of the benchmark's shapes (no public dataset).
+One step = one full MD step: bonded, IS-SPA field + force, nonbond,
+leapfrog (graph-replayed).
+
+  python bench.py [--steps K] [--warmup W] [--impl gb300|reference] [--no-batched]
+
+The gb300 arm prints one JSON line with device-timed throughput, the end-to-end
+figure through the C ABI with host buffers, the roofline of the dominant
+kernel and the CPU oracle timed on this host as a baseline.  The reference arm
+times the CPU restatement of the reference algorithm (the reference's CUDA code
+cannot be built where this runs) with all host threads on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for p in (os.path.join(ROOT, "isspa-force-cuda_gb300"), os.path.join(ROOT, "oracle")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "atom-steps/s (IS-SPA MD, plain single window, FP32)"
+UNIT = "atom-steps/s"
+DT_PS = 0.002
+L2_FLUSH = 256 << 20  # twice the 129 MB L2
+# algorithmic work per pair / point, FMA = 2 flops (fixed convention)
+FLOP_FIELD_PAIR, FLOP_FORCE_PAIR, FLOP_POINT, FLOP_NB_PAIR = 38, 88, 30, 32
+
+
+def ns_per_day(steps_per_s: float) -> float:
+    return steps_per_s * DT_PS * 1e-3 * 86400.0
+
+
+def host_cores() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int = 0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+        self.t = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            if self.t:
+                self.t.join(timeout=2)
+
+    def summary(self):
+        if not self.lines:
+            return None
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return None
+
+
+def ncu_traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    return d.get(kernel)
+
+
+def cpu_oracle_rate(system, budget_s: float, min_steps: int = 1, max_steps: int = 1000000):
+    """Full force evaluations + leapfrog of the oracle on all host cores."""
+    import oracle
+
+    oracle.build()
+    cores = host_cores()
+    o = oracle.Oracle(system, threads=cores)
+    t0 = time.perf_counter()
+    n = 0
+    while n < max_steps:
+        f, _, _ = o.total_force(seed=system.seed, step=n)
+        o.leapfrog(f, seed=system.seed, step=n)
+        n += 1
+        if n >= min_steps and time.perf_counter() - t0 >= budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return system.n_atoms * n / dt, n, dt, cores
+
+
+def run_gb300(args):
+    import build as engine_build
+    import isspa_gb300 as ig
+
+    engine_build.build()
+    sysm = ig.synth.config_plain(seed=2)
+    N, M = sysm.n_atoms, sysm.n_mc
+    P = N * M
+    eng = ig.Engine(sysm)
+    eng.step(args.warmup)
+    eng.time_steps_detailed(max(args.warmup, 3), L2_FLUSH)
+    eng.synchronize()
+    with ClockSampler(0) as clk:
+        total_ms, kern = eng.time_steps_detailed(args.steps, L2_FLUSH)
+    eng.synchronize()
+    status = eng.device_status()
+    ms_step = total_ms / args.steps
+    value = N * args.steps / (total_ms * 1e-3)
+
+    # end to end through the C ABI with pinned host buffers, copies in the timed region
+    L = ig.abi.lib()
+    import ctypes as C
+
+    nbytes = 16 * N
+    bufs = []
+    for _ in range(5):
+        ptr = C.c_void_p()
+        ig.abi.check(L.isspa_host_alloc(nbytes, C.byref(ptr)))
+        bufs.append(ptr)
+    arrs = [np.ctypeslib.as_array((C.c_float * (4 * N)).from_address(b.value)).reshape(N, 4) for b in bufs]
+    arrs[0][:] = eng.positions()
+    arrs[1][:] = eng.velocities()
+    for _ in range(3):
+        eng.step_host(arrs[0], arrs[1], arrs[2], arrs[3], arrs[4])
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        src, dst = (0, 2) if k % 2 == 0 else (2, 0)
+        eng.step_host(arrs[src], arrs[src + 1], arrs[dst], arrs[dst + 1], arrs[4])
+    e2e_s = time.perf_counter() - t0
+    e2e = N * args.steps / e2e_s
+    for b in bufs:
+        L.isspa_host_free(b)
+
+    # roofline of the dominant kernel (FP32 CUDA-core bound: the pair sums are
+    # not contractions); peak = live FMA probe on this GPU
+    flops = {"field": FLOP_FIELD_PAIR * N * P + FLOP_POINT * P, "force": FLOP_FORCE_PAIR * N * P,
+             "nonbond": FLOP_NB_PAIR * N * (N - 1)}
+    avg = {k: (v[0] / v[1]) for k, v in kern.items() if v[1] > 0}
+    dom = max(avg, key=avg.get)
+    peak_fp32 = ig.measure_fp32_peak()
+    kname = {"field": "field_kernel", "force": "force_kernel", "nonbond": "nonbond_kernel"}.get(dom, dom)
+    if dom in flops:
+        achieved = flops[dom] / (avg[dom] * 1e-3) / 1e12
+        roof = {"bound": "fp32", "achieved": round(achieved, 3), "peak": round(peak_fp32, 3),
+                "unit": "TFLOP/s", "frac": round(achieved / peak_fp32, 4),
+                "traffic": ncu_traffic(kname), "kernel": kname,
+                "peak_source": "measured FP32 FMA probe on this GPU (MEASURED_PEAKS.json has HBM and bf16 only)"}
+    else:
+        roof = {"bound": "fp32", "achieved": None, "peak": round(peak_fp32, 3), "unit": "TFLOP/s",
+                "frac": None, "traffic": None, "kernel": kname}
+    step_flops = sum(flops.values())
+    roof["step_achieved_tflops"] = round(step_flops / (ms_step * 1e-3) / 1e12, 3)
+    roof["step_frac"] = round(roof["step_achieved_tflops"] / peak_fp32, 4)
+    pk = measured_peaks()
+    hbm_bytes = 16 * N * 4 + 64 * P * 2  # pos/vel/force read+write, point records written and read once
+    roof["hbm"] = {"achieved_gbs": round(hbm_bytes / (ms_step * 1e-3) / 1e9, 2),
+                   "peak_gbs": pk.get("hbm_gbs") if pk else 6800.0,
+                   "peak_source": "MEASURED_PEAKS.json" if pk else "fallback"}
+    launches = int(sum(v[1] for v in kern.values()))
+
+    cpu_value, cpu_steps, cpu_s, cores = cpu_oracle_rate(sysm, budget_s=args.cpu_budget)
+    line = {
+        "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_step, 5), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "ns_per_day": round(ns_per_day(args.steps / (total_ms * 1e-3)), 1),
+        "config": {"workload": "plain drop-in path: 1100 atoms (50 x 22-atom chains), nMC=50, 60 A box, "
+                               "all-pairs nonbond + IS-SPA, leapfrog/Andersen 298 K, dt 2 fs",
+                   "n_atoms": N, "n_mc": M, "mc_points": P, "box_A": 60.0,
+                   "l2": "256 MB written between timed steps (outside the timed intervals)",
+                   "field_split": None, "graph": True},
+        "e2e": {"value": round(e2e, 1), "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes,
+                "d2h_bytes_per_step": 3 * nbytes},
+        "gpu_launches": launches,
+        "kernel_ms_per_launch": {k: round(v, 5) for k, v in avg.items()},
+        "roofline": roof,
+        "cpu_baseline": {"value": round(cpu_value, 1), "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{cpu_steps} full MD steps of the same 1100-atom system "
+                                   f"({cpu_s:.1f} s), CPU oracle (FP64 values), OpenMP"},
+        "device_status": status,
+    }
+    clocks = clk.summary()
+    line["clocks"] = clocks
+    if not args.no_batched:
+        line["batched"] = run_batched(ig, args, value)
+    print(json.dumps(line))
+
+
+def run_batched(ig, args, plain_value):
+    """64 umbrella windows (44..1100 atoms) in one engine vs the plain per-window path."""
+    wins = ig.synth.config_batched(n_windows=64, seed=4)
+    eng = ig.Engine(wins)
+    nat = sum(w.n_atoms for w in wins)
+    steps = max(3, args.steps // 10)
+    eng.step(3)
+    ms, kern = eng.time_steps_detailed(steps, L2_FLUSH)
+    batched = nat * steps / (ms * 1e-3)
+    # plain path: each window alone in its own engine, one after another
+    plain_ms = 0.0
+    for w in wins:
+        e1 = ig.Engine(w)
+        e1.step(2)
+        t, _ = e1.time_steps_detailed(2, 0)
+        plain_ms += t / 2
+        e1.close()
+    plain = nat / (plain_ms * 1e-3)
+    eng.close()
+    return {"windows": len(wins), "atoms_total": nat, "steps": steps,
+            "value": round(batched, 1), "unit": UNIT, "ms_per_step": round(ms / steps, 4),
+            "plain_per_window_value": round(plain, 1), "speedup_vs_plain": round(batched / plain, 2)}
+
+
+def run_reference(args):
+    """CPU restatement of the reference path, all host threads, same workload."""
+    import isspa_gb300.synth as synth
+
+    sysm = synth.config_plain(seed=2)
+    budget = args.cpu_budget * 3
+    value, n, dt, cores = cpu_oracle_rate(sysm, budget_s=budget, min_steps=1,
+                                          max_steps=max(1, args.steps + args.warmup))
+    line = {"impl": "reference", "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": 1,
+            "steps": n, "warmup": 0, "ms_per_step": round(dt / n * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "plain drop-in path: 1100 atoms (50 x 22-atom chains), nMC=50, 60 A box",
+                       "n_atoms": sysm.n_atoms, "n_mc": sysm.n_mc},
+            "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{n} full MD steps ({dt:.1f} s) of the CPU restatement of the "
+                                       "reference kernels; the reference CUDA build needs its source "
+                                       "tree, which is not present here"},
+            "e2e": {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_profile_case(args):
+    """Untimed graph steps of a workload, for ncu launch lists and captures."""
+    import build as engine_build
+    import isspa_gb300 as ig
+
+    engine_build.build()
+    if args.workload == "batched":
+        eng = ig.Engine(ig.synth.config_batched(n_windows=64, seed=4))
+    elif args.workload == "precision":
+        eng = ig.Engine(ig.synth.config_precision(seed=3))
+    else:
+        eng = ig.Engine(ig.synth.config_plain(seed=2))
+    eng.step(args.profile_steps)
+    eng.synchronize()
+    print(json.dumps({"profile_case": args.workload, "steps": args.profile_steps, "atoms": eng.n_atoms,
+                      "points": eng.n_points}))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--profile-steps", type=int, default=0,
+                    help="run this many untimed graph steps and exit (profiling case)")
+    ap.add_argument("--workload", default="plain", choices=["plain", "batched", "precision"])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--no-batched", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return  # replicas only: the engine runs on one GPU; other ranks do no work
+    if args.profile_steps > 0:
+        run_profile_case(args)
+    elif args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -114,6 +114,8 @@ typedef struct isspa_host_system isspa_host_system;
 
 const char *isspa_strerror(int status);
 void isspa_default_options(isspa_engine_options *opt);
+/* Number of CUDA devices visible to this process (0 when there is none). */
+int isspa_device_count(int *count);
 
 /* ---- input files (host side, no GPU needed) ------------------------------ */
 /* Parsed `key = value` run configuration (config_class.cpp:14-133). */
@@ -175,6 +177,17 @@ int isspa_step(isspa_engine *e, int nsteps);
  * stream).  flush_bytes > 0 writes that many bytes of scratch between steps
  * (outside the timed intervals) to evict L2. */
 int isspa_time_steps(isspa_engine *e, int nsteps, size_t flush_bytes, double *ms_total);
+/* As isspa_time_steps, also timing every kernel of the step with CUDA events
+ * recorded on the stream each kernel runs on, inside the replayed graph.
+ * ms_kernels[ISSPA_K_COUNT] receives the summed milliseconds per kernel and
+ * launches[ISSPA_K_COUNT] the number of launches of each. */
+enum { ISSPA_K_FIELD = 0, ISSPA_K_FORCE, ISSPA_K_NONBOND, ISSPA_K_BONDED, ISSPA_K_UMBRELLA,
+       ISSPA_K_LEAPFROG, ISSPA_K_COUNT };
+int isspa_time_steps_detailed(isspa_engine *e, int nsteps, size_t flush_bytes, double *ms_total,
+                              double *ms_kernels, int *launches);
+/* Page-locked host buffers for host<->device transfers (cudaMallocHost). */
+int isspa_host_alloc(size_t bytes, void **out);
+void isspa_host_free(void *p);
 int isspa_synchronize(isspa_engine *e);
 /* Sticky device status word (0 if nothing tripped); clears it when reset != 0. */
 int isspa_device_status(isspa_engine *e, int reset);

@@ -122,7 +122,10 @@ struct isspa_engine {
         if (stream) cudaStreamSynchronize(stream);
         if (graph1) cudaGraphExecDestroy(graph1);
         if (graphN) cudaGraphExecDestroy(graphN);
+        if (graph_timed) cudaGraphExecDestroy(graph_timed);
         for (auto ev : tev) cudaEventDestroy(ev);
+        for (auto ev : kev)
+            if (ev) cudaEventDestroy(ev);
         for (cudaEvent_t ev : {ev_fork, ev_join, ev_a, ev_b})
             if (ev) cudaEventDestroy(ev);
         for (void *p : allocs) cudaFree(p);
@@ -268,24 +271,57 @@ struct isspa_engine {
         launch_umbrella(umbrella_args(), s);
         launch_leapfrog(leapfrog_args(), s);
     }
+    // Which kernels a step launches (the wrappers skip empty work lists).
+    bool launches(int k) const {
+        switch (k) {
+            case ISSPA_K_FIELD: return n_field_tiles > 0;
+            case ISSPA_K_FORCE: return n_force_items > 0;
+            case ISSPA_K_NONBOND: return n_nb_items > 0;
+            case ISSPA_K_BONDED: return n_bonds + n_angles + n_dihs > 0;
+            case ISSPA_K_UMBRELLA: return n_us > 0;
+            case ISSPA_K_LEAPFROG: return n_atoms > 0;
+        }
+        return false;
+    }
     // Step with the two independent chains (field->force and bonded, umbrella,
-    // nonbond) on forked streams; both add into the same accumulator.
-    void enqueue_step_forked() {
+    // nonbond) on forked streams; both add into the same accumulator.  With
+    // `timed`, CUDA events bracket every kernel on the stream it runs on.
+    void enqueue_step_forked(bool timed = false) {
+        // External event-record nodes: a plain cudaEventRecord under capture only
+        // orders the graph and is never recorded at replay time.
+        auto mark = [&](int k, int end, cudaStream_t s) {
+            if (timed && launches(k)) ck(cudaEventRecordWithFlags(kev[2 * k + end], s, cudaEventRecordExternal));
+        };
         ck(cudaEventRecord(ev_fork, stream));
         ck(cudaStreamWaitEvent(side, ev_fork, 0));
-        enqueue_isspa(stream);
+        mark(ISSPA_K_FIELD, 0, stream);
+        launch_field(field_args(), field_split, false, stream);
+        mark(ISSPA_K_FIELD, 1, stream);
+        mark(ISSPA_K_FORCE, 0, stream);
+        launch_force(force_args(), stream);
+        mark(ISSPA_K_FORCE, 1, stream);
+        mark(ISSPA_K_BONDED, 0, side);
         launch_bonded(bonded_args(1, 1, 1), side);
+        mark(ISSPA_K_BONDED, 1, side);
+        mark(ISSPA_K_UMBRELLA, 0, side);
         launch_umbrella(umbrella_args(), side);
+        mark(ISSPA_K_UMBRELLA, 1, side);
+        mark(ISSPA_K_NONBOND, 0, side);
         launch_nonbond(nonbond_args(), side);
+        mark(ISSPA_K_NONBOND, 1, side);
         ck(cudaEventRecord(ev_join, side));
         ck(cudaStreamWaitEvent(stream, ev_join, 0));
+        mark(ISSPA_K_LEAPFROG, 0, stream);
         launch_leapfrog(leapfrog_args(), stream);
+        mark(ISSPA_K_LEAPFROG, 1, stream);
     }
-    cudaGraphExec_t capture(int nsteps) {
+    cudaEvent_t kev[2 * ISSPA_K_COUNT] = {};
+    cudaGraphExec_t graph_timed = nullptr;
+    cudaGraphExec_t capture(int nsteps, bool timed = false) {
         cudaGraph_t g = nullptr;
         ck(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
         try {
-            for (int k = 0; k < nsteps; ++k) enqueue_step_forked();
+            for (int k = 0; k < nsteps; ++k) enqueue_step_forked(timed);
         } catch (...) {
             cudaStreamEndCapture(stream, &g);
             if (g) cudaGraphDestroy(g);
@@ -301,7 +337,8 @@ struct isspa_engine {
     void invalidate_graphs() {
         if (graph1) cudaGraphExecDestroy(graph1);
         if (graphN) cudaGraphExecDestroy(graphN);
-        graph1 = graphN = nullptr;
+        if (graph_timed) cudaGraphExecDestroy(graph_timed);
+        graph1 = graphN = graph_timed = nullptr;
     }
     void run_steps(int nsteps) {
         if (!opt.use_graph) {
@@ -676,6 +713,17 @@ const char *isspa_strerror(int s) {
     }
 }
 
+int isspa_device_count(int *count) {
+    if (!count) return ISSPA_ERR_ARG;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        n = 0;
+    }
+    *count = n;
+    return ISSPA_OK;
+}
+
 void isspa_default_options(isspa_engine_options *o) {
     if (!o) return;
     std::memset(o, 0, sizeof *o);
@@ -803,6 +851,68 @@ int isspa_time_steps(isspa_engine *e, int nsteps, size_t flush_bytes, double *ms
         }
         *ms_total = tot;
     });
+}
+
+int isspa_time_steps_detailed(isspa_engine *e, int nsteps, size_t flush_bytes, double *ms_total,
+                              double *ms_kernels, int *launches) {
+    if (nsteps <= 0 || !ms_total || !ms_kernels || !launches) return ISSPA_ERR_ARG;
+    int rc = guard(e);
+    if (rc) return rc;
+    return run_guarded([&] {
+        if (flush_bytes && flush_bytes != e->flush_bytes) {
+            if (e->flush) {
+                cudaFree(e->flush);
+                e->flush = nullptr;
+            }
+            ck(cudaMalloc(&e->flush, flush_bytes));
+            e->flush_bytes = flush_bytes;
+        }
+        if (!e->kev[0])
+            for (auto &ev : e->kev) ck(cudaEventCreate(&ev));
+        while (e->tev.size() < 2) {
+            cudaEvent_t ev;
+            ck(cudaEventCreate(&ev));
+            e->tev.push_back(ev);
+        }
+        if (!e->graph_timed) e->graph_timed = e->capture(1, true);
+        double tot = 0.0, kt[ISSPA_K_COUNT] = {0};
+        int kl[ISSPA_K_COUNT] = {0};
+        for (int s = 0; s < nsteps; ++s) {
+            if (flush_bytes) ck(cudaMemsetAsync(e->flush, s & 0xff, flush_bytes, e->stream));
+            ck(cudaEventRecord(e->tev[0], e->stream));
+            ck(cudaGraphLaunch(e->graph_timed, e->stream));
+            ck(cudaEventRecord(e->tev[1], e->stream));
+            ck(cudaStreamSynchronize(e->stream));
+            float ms = 0.f;
+            ck(cudaEventElapsedTime(&ms, e->tev[0], e->tev[1]));
+            tot += ms;
+            for (int k = 0; k < ISSPA_K_COUNT; ++k) {
+                if (!e->launches(k)) continue;
+                ck(cudaEventElapsedTime(&ms, e->kev[2 * k], e->kev[2 * k + 1]));
+                kt[k] += ms;
+                kl[k] += 1;
+            }
+        }
+        *ms_total = tot;
+        for (int k = 0; k < ISSPA_K_COUNT; ++k) {
+            ms_kernels[k] = kt[k];
+            launches[k] = kl[k];
+        }
+    });
+}
+
+int isspa_host_alloc(size_t bytes, void **out) {
+    if (!out || !bytes) return ISSPA_ERR_ARG;
+    if (cudaMallocHost(out, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        *out = nullptr;
+        return ISSPA_ERR_NOMEM;
+    }
+    return ISSPA_OK;
+}
+
+void isspa_host_free(void *p) {
+    if (p) cudaFreeHost(p);
 }
 
 int isspa_synchronize(isspa_engine *e) {

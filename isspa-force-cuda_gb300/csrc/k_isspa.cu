@@ -228,10 +228,15 @@ __global__ void __launch_bounds__(kForceThreads) force_kernel(ForceArgs a) {
     const float f_r0 = a.f_r0, f_dr = a.f_dr, f_inv = a.f_inv;
     const int nf = a.n_f;
 
-    float qx = 0.f, qy = 0.f, qz = 0.f;  // terms proportional to -q_i vtot_i
-    float lx = 0.f, ly = 0.f, lz = 0.f;  // tabulated LJ, proportional to -vtot_i
+    const float vt = __ldg(a.vtot + ity);
+    // Per-stage FP32 partial sums (at most kForceThreads points) are folded into
+    // per-thread fixed-point registers, so FP32 rounding never spans more than
+    // one stage; one set of atomics per work item.
+    long long fxa = 0, fya = 0, fza = 0;
 
     for (int p0 = 0; p0 < ch.y; p0 += kForceThreads) {
+        float qx = 0.f, qy = 0.f, qz = 0.f;  // terms proportional to -q_i vtot_i
+        float lx = 0.f, ly = 0.f, lz = 0.f;  // tabulated LJ, proportional to -vtot_i
         const int pn = min(kForceThreads, ch.y - p0);
         __syncthreads();
         if (t < pn) {
@@ -290,14 +295,19 @@ __global__ void __launch_bounds__(kForceThreads) force_kernel(ForceArgs a) {
                 qz = fmaf(tc, fmaf(pd, rz, -E0.z), qz);
             }
         }
+        const float Fx = -vt * fmaf(xi.w, qx, lx);
+        const float Fy = -vt * fmaf(xi.w, qy, ly);
+        const float Fz = -vt * fmaf(xi.w, qz, lz);
+        if (active) check_force(a.status, Fx, Fy, Fz);
+        fxa += to_fix(Fx);
+        fya += to_fix(Fy);
+        fza += to_fix(Fz);
     }
     if (!active) return;
-    const float vt = __ldg(a.vtot + ity);
-    const float Fx = -vt * fmaf(xi.w, qx, lx);
-    const float Fy = -vt * fmaf(xi.w, qy, ly);
-    const float Fz = -vt * fmaf(xi.w, qz, lz);
-    check_force(a.status, Fx, Fy, Fz);
-    fix_add3(a.facc + 3 * (long long)ai, Fx, Fy, Fz);
+    unsigned long long *acc = a.facc + 3 * (long long)ai;
+    atomicAdd(acc + 0, (unsigned long long)fxa);
+    atomicAdd(acc + 1, (unsigned long long)fya);
+    atomicAdd(acc + 2, (unsigned long long)fza);
 }
 
 template <int S, bool GEN, bool RAW>

@@ -50,9 +50,10 @@ __global__ void __launch_bounds__(kNbThreads) nonbond_kernel(NonbondArgs a) {
     while (cur < end && a.excl[cur] < item.w) ++cur;
     int next_ex = cur < end ? a.excl[cur] : INT_MAX;
 
-    float ax = 0.f, ay = 0.f, az = 0.f;
+    long long fxa = 0, fya = 0, fza = 0;  // per-stage partial sums in fixed point
     for (int j0 = 0; j0 < nj; j0 += kNbThreads) {
         const int jn = min(kNbThreads, nj - j0);
+        float ax = 0.f, ay = 0.f, az = 0.f;
         __syncthreads();
         if (t < jn) {
             const int j = item.w + j0 + t;
@@ -98,10 +99,16 @@ __global__ void __launch_bounds__(kNbThreads) nonbond_kernel(NonbondArgs a) {
             ay = fmaf(fs, ry, ay);
             az = fmaf(fs, rz, az);
         }
+        if (active) check_force(a.status, ax, ay, az);
+        fxa += to_fix(ax);
+        fya += to_fix(ay);
+        fza += to_fix(az);
     }
     if (!active) return;
-    check_force(a.status, ax, ay, az);
-    fix_add3(a.facc + 3 * (long long)i, ax, ay, az);
+    unsigned long long *acc = a.facc + 3 * (long long)i;
+    atomicAdd(acc + 0, (unsigned long long)fxa);
+    atomicAdd(acc + 1, (unsigned long long)fya);
+    atomicAdd(acc + 2, (unsigned long long)fza);
 }
 
 __device__ __forceinline__ float3 rvec(const float4 *pos, int p, int q, float L, float h) {

@@ -68,6 +68,7 @@ _FP = C.POINTER(C.c_float)
 SIGNATURES = [
     ("isspa_strerror", C.c_char_p, [C.c_int]),
     ("isspa_default_options", None, [C.POINTER(EngineOptions)]),
+    ("isspa_device_count", C.c_int, [C.POINTER(C.c_int)]),
     ("isspa_read_run_config", C.c_int, [C.c_char_p, C.POINTER(RunConfig)]),
     ("isspa_system_load", C.c_int, [C.POINTER(RunConfig), C.c_char_p, C.POINTER(_P)]),
     ("isspa_read_prmtop", C.c_int, [C.c_char_p, C.c_float, C.POINTER(_P)]),
@@ -90,6 +91,10 @@ SIGNATURES = [
     ("leapfrog_cuda", C.c_int, [_P, _FP]),
     ("isspa_step", C.c_int, [_P, C.c_int]),
     ("isspa_time_steps", C.c_int, [_P, C.c_int, C.c_size_t, C.POINTER(C.c_double)]),
+    ("isspa_time_steps_detailed", C.c_int, [_P, C.c_int, C.c_size_t, C.POINTER(C.c_double),
+                                            C.POINTER(C.c_double), C.POINTER(C.c_int)]),
+    ("isspa_host_alloc", C.c_int, [C.c_size_t, C.POINTER(_P)]),
+    ("isspa_host_free", None, [_P]),
     ("isspa_synchronize", C.c_int, [_P]),
     ("isspa_device_status", C.c_int, [_P, C.c_int]),
     ("isspa_set_positions", C.c_int, [_P, _P, C.c_int]),
@@ -130,3 +135,9 @@ def lib():
 def check(status: int, what: str = "") -> None:
     if status != OK:
         raise IsspaError(status, what)
+
+
+def device_count() -> int:
+    n = C.c_int(0)
+    lib().isspa_device_count(C.byref(n))
+    return n.value

@@ -113,6 +113,17 @@ class Engine:
         abi.check(abi.lib().isspa_time_steps(self._h, int(nsteps), int(flush_bytes), C.byref(ms)), "time")
         return ms.value
 
+    KERNELS = ("field", "force", "nonbond", "bonded", "umbrella", "leapfrog")
+
+    def time_steps_detailed(self, nsteps: int, flush_bytes: int = 0):
+        """Device time of `nsteps` graph-replayed steps and of every kernel in them."""
+        tot = C.c_double(0.0)
+        kms = (C.c_double * len(self.KERNELS))()
+        kn = (C.c_int * len(self.KERNELS))()
+        abi.check(abi.lib().isspa_time_steps_detailed(self._h, int(nsteps), int(flush_bytes), C.byref(tot),
+                                                       kms, kn), "time detailed")
+        return tot.value, {k: (kms[i], kn[i]) for i, k in enumerate(self.KERNELS)}
+
     def synchronize(self):
         abi.check(abi.lib().isspa_synchronize(self._h), "synchronize")
 

@@ -171,24 +171,39 @@ void orc_field(const orc_isspa_sys *s, int n_mc, const float *pts, double *w, in
 
 /* Langevin averages for a dipole in field x: <P1>=coth x-1/x (c1 of
  * isspa_force_cuda.cu:271), <P2>=1.5*c2-0.5 (:283), <P3>=2.5*c3-1.5*c1 (:287).
- * The closed forms cancel catastrophically as x->0; below 0.25 the Taylor
- * series of the same functions is used. */
+ * The closed forms cancel catastrophically as x->0.  These averages are the
+ * ratios i_l(x)/i_0(x) of modified spherical Bessel functions; below 5 they
+ * are evaluated from the backward continued fraction of i_l/i_(l-1),
+ * r_l = x / (2l+1 + x r_(l+1)), whose terms are all positive. */
+static int g_langevin_float_closed = 0;
+
+/* Diagnostic mode: evaluate the averages as the reference does, with its closed
+ * forms in float (isspa_force_cuda.cu:270-273), to measure what their
+ * cancellation does to the mean force. */
+void orc_set_langevin_mode(int float_closed_forms) { g_langevin_float_closed = float_closed_forms; }
+
 void orc_langevin(double x, double out[3]) {
-    if (x < 0.25) {
-        const double x2 = x * x;
-        static const double a1[] = {1.0 / 3, -1.0 / 45, 2.0 / 945, -1.0 / 4725, 2.0 / 93555,
-                                    -1382.0 / 638512875, 4.0 / 18243225};
-        static const double a2[] = {1.0 / 15, -2.0 / 315, 1.0 / 1575, -2.0 / 31185,
-                                    1382.0 / 212837625, -4.0 / 6081075};
-        static const double a3[] = {1.0 / 105, -1.0 / 945, 17.0 / 155925, -472.0 / 42567525,
-                                    718.0 / 638512875, -1237.0 / 10854718875.0};
-        double s1 = 0, s2 = 0, s3 = 0;
-        for (int k = 6; k >= 0; --k) s1 = s1 * x2 + a1[k];
-        for (int k = 5; k >= 0; --k) s2 = s2 * x2 + a2[k];
-        for (int k = 5; k >= 0; --k) s3 = s3 * x2 + a3[k];
-        out[0] = x * s1;
-        out[1] = x2 * s2;
-        out[2] = x2 * x * s3;
+    if (g_langevin_float_closed) {
+        const float xf = (float)x;
+        const float cothE = 1.0f / tanhf(xf);
+        const float c1 = cothE - 1.0f / xf;
+        const float c2 = 1.0f - 2.0f * (c1 / xf);
+        const float c3 = cothE - 3.0f * (c2 / xf);
+        out[0] = c1;
+        out[1] = 1.5f * c2 - 0.5f;
+        out[2] = 2.5f * c3 - 1.5f * c1;
+        return;
+    }
+    if (x < 5.0) {
+        double r = 0.0, r2 = 0.0, r3 = 0.0;
+        for (int l = 40; l >= 1; --l) {
+            r = x / ((double)(2 * l + 1) + x * r);
+            if (l == 3) r3 = r;
+            if (l == 2) r2 = r;
+        }
+        out[0] = r;
+        out[1] = r * r2;
+        out[2] = r * r2 * r3;
         return;
     }
     const double coth = 1.0 / tanh(x);

@@ -87,6 +87,8 @@ void orc_isspa_force(const orc_isspa_sys *s, int n_mc, const float *pts, const d
 
 /* Langevin polarisation averages <P1>, <P2>, <P3> for field magnitude x. */
 void orc_langevin(double x, double out[3]);
+/* 1: evaluate them with the reference's float closed forms (diagnostic). */
+void orc_set_langevin_mode(int float_closed_forms);
 
 /* All-pairs LJ + Coulomb + IS-SPA correction (nonbond_force_cuda.cu:31-174). */
 void orc_nonbond(const orc_nb_sys *s, int term_mask, double *f /* [N][3] += */);
