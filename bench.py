@@ -157,6 +157,7 @@ def run_gb300(args):
     N, M = sysm.n_atoms, sysm.n_mc
     P = N * M
     eng = ig.Engine(sysm)
+    shapes = eng.shapes()
     eng.step(args.warmup)
     eng.time_steps_detailed(max(args.warmup, 3), L2_FLUSH)
     eng.synchronize()
@@ -228,7 +229,7 @@ def run_gb300(args):
                                "all-pairs nonbond + IS-SPA, leapfrog/Andersen 298 K, dt 2 fs",
                    "n_atoms": N, "n_mc": M, "mc_points": P, "box_A": 60.0,
                    "l2": "256 MB written between timed steps (outside the timed intervals)",
-                   "field_split": None, "graph": True},
+                   "launch_shapes": shapes, "graph": True},
         "e2e": {"value": round(e2e, 1), "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes,
                 "d2h_bytes_per_step": 3 * nbytes},
         "gpu_launches": launches,
@@ -315,7 +316,7 @@ def main():
                     help="run this many untimed graph steps and exit (profiling case)")
     ap.add_argument("--workload", default="plain", choices=["plain", "batched", "precision"])
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=15.0)

@@ -155,6 +155,11 @@ int isspa_engine_create(const isspa_system_desc *windows, int n_windows,
 void isspa_engine_destroy(isspa_engine *e);
 int isspa_engine_info(const isspa_engine *e, int *n_windows, int *n_atoms_total,
                       long long *n_points_total);
+/* Launch shapes the engine chose (or was given) for its work lists:
+ * shape[0] field atom-loop split, [1] field tiles, [2] force points per work
+ * item, [3] force work items, [4] nonbond work items, [5] nonbond partners per
+ * item, [6] SM count used for the choice. */
+int isspa_engine_shapes(const isspa_engine *e, int shape[7]);
 
 /* ---- per-step force calls (reference names and order) -------------------- */
 /* Each call adds its forces into the engine's force accumulator, exactly as the

@@ -67,7 +67,7 @@ struct isspa_engine {
     int n_force_items = 0, force_chunk = 0;
     int4 *nb_items = nullptr;
     int *nb_nj = nullptr;
-    int n_nb_items = 0;
+    int n_nb_items = 0, nb_chunk = 0, n_sms = 0;
     int4 *bonds = nullptr, *angles = nullptr, *dihs = nullptr;
     float2 *bond_par = nullptr, *angle_par = nullptr, *sc14 = nullptr;
     float4 *dih_par = nullptr;
@@ -548,17 +548,36 @@ void build(isspa_engine &E, const std::vector<isspa_host_system> &ws) {
     for (int w = 0; w < W; ++w) order[w] = w;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return ws[a].n_atoms > ws[b].n_atoms; });
     // field tiles: S warps split the atom loop of 128/S points
-    const int slots = 2432;  // 152 SMs x 16 resident 128-thread blocks
+    // Launch shapes are chosen so that grids fill whole waves of resident
+    // blocks (the tail wave of an equal-work grid idles the other SMs).
+    int dev = 0, sms = 0;
+    ck(cudaGetDevice(&dev));
+    ck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    auto wave_eff = [](long long units, long long slots) {
+        if (slots <= 0) return 0.0;
+        const double waves = (double)units / (double)slots;
+        return waves / std::ceil(waves);
+    };
     auto tiles_for = [&](int S) {
+        const int tp = field_points_per_block(S);
         long long n = 0;
-        for (int w = 0; w < W; ++w) n += ((long long)ws[w].n_atoms * E.n_mc + 128 / S - 1) / (128 / S);
+        for (int w = 0; w < W; ++w) n += ((long long)ws[w].n_atoms * E.n_mc + tp - 1) / tp;
         return n;
     };
     int S = E.opt.field_split;
-    if (S != 1 && S != 2 && S != 4) S = tiles_for(1) >= slots ? 1 : (tiles_for(2) >= slots ? 2 : 4);
+    if (S != 1 && S != 2 && S != 4 && S != 8 && S != 16) {
+        double best = -1.0;
+        for (int cand : {1, 2, 4, 8, 16}) {
+            const double e = wave_eff(tiles_for(cand), (long long)sms * field_blocks_per_sm(cand));
+            if (e > best + 0.02) {
+                best = e;
+                S = cand;
+            }
+        }
+    }
     E.field_split = S;
     std::vector<int4> ftiles;
-    const int tp = 128 / S;
+    const int tp = field_points_per_block(S);
     for (int w : order) {
         long long P = (long long)ws[w].n_atoms * E.n_mc;
         for (long long p = 0; p < P; p += tp)
@@ -566,15 +585,26 @@ void build(isspa_engine &E, const std::vector<isspa_host_system> &ws) {
     }
     if (E.n_points > INT32_MAX) throw Fail{ISSPA_ERR_UNSUPPORTED};
     E.n_field_tiles = (int)ftiles.size();
-    // force items: 128-atom tiles x point chunks
-    long long pairs = 0;
-    for (int w = 0; w < W; ++w) pairs += (long long)ws[w].n_atoms * ws[w].n_atoms * E.n_mc;
+    // force items: 128-atom tiles x point chunks of C points
+    auto items_for = [&](long long C) {
+        long long n = 0;
+        for (int w = 0; w < W; ++w)
+            n += ((ws[w].n_atoms + 127) / 128) * (((long long)ws[w].n_atoms * E.n_mc + C - 1) / C);
+        return n;
+    };
     int C = E.opt.force_chunk;
     if (C <= 0) {
-        long long target = 4 * (long long)slots;
-        long long c = pairs / (128LL * target);
-        c = std::max<long long>(128, std::min<long long>(8192, ((c + 127) / 128) * 128));
-        C = (int)c;
+        const long long fslots = (long long)sms * std::max(1, force_blocks_per_sm());
+        double best = -1.0;
+        C = 64;
+        for (long long c = 8192; c >= 64; c -= 32) {  // prefer long chunks (fewer atomics) at equal efficiency
+            const long long n = items_for(c);
+            const double e = n < fslots ? 0.5 * (double)n / (double)fslots : wave_eff(n, fslots);
+            if (e > best + 0.01) {
+                best = e;
+                C = (int)c;
+            }
+        }
     }
     E.force_chunk = C;
     std::vector<int4> fitems;
@@ -606,6 +636,8 @@ void build(isspa_engine &E, const std::vector<isspa_host_system> &ws) {
             }
     }
     E.n_nb_items = (int)nitems.size();
+    E.nb_chunk = J;
+    E.n_sms = sms;
 
     // ---- upload ----
     E.pos = E.upload(pos);
@@ -782,6 +814,18 @@ int isspa_engine_info(const isspa_engine *e, int *nw, int *na, long long *np) {
     if (nw) *nw = e->n_windows;
     if (na) *na = e->n_atoms;
     if (np) *np = e->n_points;
+    return ISSPA_OK;
+}
+
+int isspa_engine_shapes(const isspa_engine *e, int shape[7]) {
+    if (!e || !shape) return ISSPA_ERR_ARG;
+    shape[0] = e->field_split;
+    shape[1] = e->n_field_tiles;
+    shape[2] = e->force_chunk;
+    shape[3] = e->n_force_items;
+    shape[4] = e->n_nb_items;
+    shape[5] = e->nb_chunk;
+    shape[6] = e->n_sms;
     return ISSPA_OK;
 }
 

@@ -77,12 +77,20 @@ __device__ __forceinline__ void mc_point(uint32_t p, uint32_t window, uint32_t s
     pz = __fmaf_rn(mz, rm, xa.z);
 }
 
+// Block shape of the field kernel: S warps split the atom loop of each group
+// of 32 points; 4 warps per block up to S = 4, then 32*S threads.
+template <int S>
+struct FieldShape {
+    static constexpr int kThreads = S >= 4 ? 32 * S : kFieldThreads;
+    static constexpr int kGroups = kThreads / (32 * S);  // groups of 32 points per block
+};
+
 template <int S, bool GEN, bool RAW>
-__global__ void __launch_bounds__(kFieldThreads) field_kernel(FieldArgs a) {
-    constexpr int kGroups = 4 / S;  // groups of 32 points per block
-    __shared__ float4 s_atom[kFieldThreads];
-    __shared__ int s_row[kFieldThreads];
-    __shared__ float s_red[S > 1 ? 8 : 1][kFieldThreads];
+__global__ void __launch_bounds__(FieldShape<S>::kThreads) field_kernel(FieldArgs a) {
+    constexpr int kT = FieldShape<S>::kThreads;
+    __shared__ float4 s_atom[kT];
+    __shared__ int s_row[kT];
+    __shared__ float s_red[S > 1 ? 8 : 1][kT];
 
     const int4 tile = a.tiles[blockIdx.x];
     const WinDev W = a.win[tile.x];
@@ -114,8 +122,8 @@ __global__ void __launch_bounds__(kFieldThreads) field_kernel(FieldArgs a) {
     const float e_r0 = a.e_r0, e_dr = a.e_dr, e_inv = a.e_inv;
     const int nb = a.n_gbins;
 
-    for (int j0 = 0; j0 < W.n_atoms; j0 += kFieldThreads) {
-        const int jn = min(kFieldThreads, W.n_atoms - j0);
+    for (int j0 = 0; j0 < W.n_atoms; j0 += kT) {
+        const int jn = min(kT, W.n_atoms - j0);
         __syncthreads();
         if (threadIdx.x < jn) {
             const int j = W.atom_off + j0 + threadIdx.x;
@@ -134,11 +142,13 @@ __global__ void __launch_bounds__(kFieldThreads) field_kernel(FieldArgs a) {
             const float d2 = dist2f(rx, ry, rz);
             const float ri = rsqrtf(d2);
             const float c = xj.w * (ri * ri * ri);
-            ex = fmaf(-c, rx, ex);
-            ey = fmaf(-c, ry, ey);
-            ez = fmaf(-c, rz, ez);
+            // ex.. accumulates the in-range contributions (Coulomb and tabulated
+            // field), fx.. the out-of-range Coulomb field E0; E = ex.. + fx..
             if (d2 <= rm2) {  // inside rmax of the owner's type (:154)
                 ++n;
+                ex = fmaf(-c, rx, ex);
+                ey = fmaf(-c, ry, ey);
+                ez = fmaf(-c, rz, ez);
                 const float dist = __fsqrt_rn(d2);
                 const int bin = (int)__fmul_rn(__fsub_rn(dist, g_r0), g_inv);
                 if (bin < 0) {
@@ -186,6 +196,9 @@ __global__ void __launch_bounds__(kFieldThreads) field_kernel(FieldArgs a) {
         }
     }
     if (!valid) return;
+    ex += fx;  // total mean field = in-range part + out-of-range Coulomb part
+    ey += fy;
+    ez += fz;
 
     if (RAW) {
         a.raw_e[pg] = make_float4(ex, ey, ez, w);
@@ -312,7 +325,7 @@ __global__ void __launch_bounds__(kForceThreads) force_kernel(ForceArgs a) {
 
 template <int S, bool GEN, bool RAW>
 void launch_field_t(const FieldArgs &a, cudaStream_t s) {
-    field_kernel<S, GEN, RAW><<<a.n_tiles, kFieldThreads, 0, s>>>(a);
+    field_kernel<S, GEN, RAW><<<a.n_tiles, FieldShape<S>::kThreads, 0, s>>>(a);
 }
 
 template <int S>
@@ -324,6 +337,13 @@ void launch_field_s(const FieldArgs &a, bool raw, cudaStream_t s) {
     else launch_field_t<S, false, true>(a, s);
 }
 
+template <int S>
+int field_bps() {
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, field_kernel<S, true, false>, FieldShape<S>::kThreads, 0);
+    return n;
+}
+
 }  // namespace
 
 int field_block_threads() { return kFieldThreads; }
@@ -331,9 +351,31 @@ int force_block_threads() { return kForceThreads; }
 
 void launch_field(const FieldArgs &a, int split, bool raw, cudaStream_t s) {
     if (a.n_tiles <= 0) return;
-    if (split == 4) launch_field_s<4>(a, raw, s);
-    else if (split == 2) launch_field_s<2>(a, raw, s);
-    else launch_field_s<1>(a, raw, s);
+    switch (split) {
+        case 16: launch_field_s<16>(a, raw, s); break;
+        case 8: launch_field_s<8>(a, raw, s); break;
+        case 4: launch_field_s<4>(a, raw, s); break;
+        case 2: launch_field_s<2>(a, raw, s); break;
+        default: launch_field_s<1>(a, raw, s); break;
+    }
+}
+
+int field_points_per_block(int split) { return split >= 4 ? 32 : 128 / split; }
+
+int field_blocks_per_sm(int split) {
+    switch (split) {
+        case 16: return field_bps<16>();
+        case 8: return field_bps<8>();
+        case 4: return field_bps<4>();
+        case 2: return field_bps<2>();
+        default: return field_bps<1>();
+    }
+}
+
+int force_blocks_per_sm() {
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, force_kernel<7>, kForceThreads, 0);
+    return n;
 }
 
 void launch_force(const ForceArgs &a, cudaStream_t s) {

@@ -111,29 +111,38 @@ __global__ void __launch_bounds__(kNbThreads) nonbond_kernel(NonbondArgs a) {
     atomicAdd(acc + 2, (unsigned long long)fza);
 }
 
-__device__ __forceinline__ float3 rvec(const float4 *pos, int p, int q, float L, float h) {
+// Image vector in float (the reference's minimum-image decision), then the
+// bonded arithmetic in FP64: these terms are O(N) work, and acos / 1/sin(phi)
+// / 1/|r12 x r23| make the FP32 formulas ill-conditioned for near-planar or
+// near-linear geometries.
+__device__ __forceinline__ double3 rvec(const float4 *pos, int p, int q, float L, float h) {
     const float4 a = pos[p], b = pos[q];
-    return make_float3(mimg(a.x - b.x, L, h), mimg(a.y - b.y, L, h), mimg(a.z - b.z, L, h));
+    return make_double3(mimg(a.x - b.x, L, h), mimg(a.y - b.y, L, h), mimg(a.z - b.z, L, h));
 }
 
-__device__ __forceinline__ void add_force(unsigned long long *facc, int *status, int atom, float fx,
-                                          float fy, float fz) {
-    check_force(status, fx, fy, fz);
-    fix_add3(facc + 3 * (long long)atom, fx, fy, fz);
+__device__ __forceinline__ void add_force(unsigned long long *facc, int *status, int atom, double fx,
+                                          double fy, double fz) {
+    const double m = fmax(fabs(fx), fmax(fabs(fy), fabs(fz)));
+    if (!(m <= (double)kFixLimit)) atomicOr(status, (m != m || isinf(m)) ? kStatusNonFinite : kStatusOverflow);
+    unsigned long long *acc = facc + 3 * (long long)atom;
+    atomicAdd(acc + 0, (unsigned long long)__double2ll_rn(fx * 4294967296.0));
+    atomicAdd(acc + 1, (unsigned long long)__double2ll_rn(fy * 4294967296.0));
+    atomicAdd(acc + 2, (unsigned long long)__double2ll_rn(fz * 4294967296.0));
 }
+
+__device__ __forceinline__ double dot3(double3 a, double3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 
 __global__ void bonded_kernel(BondedArgs a) {
     long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long nb = a.do_bonds ? a.n_bonds : 0;
     const long long na = a.do_angles ? a.n_angles : 0;
     const long long nd = a.do_dihs ? a.n_dihs : 0;
-    if (idx < nb) {  // bond_force_cuda.cu:36-50
+    if (idx < nb) {  // bond_force_cuda.cu:36-50: f = 2k (r0/|r| - 1) r on atom x
         const int4 b = a.bonds[idx];
         const WinDev W = a.win[a.atom_win[b.x]];
-        const float3 r = rvec(a.pos, b.x, b.y, W.box, W.hbox);
+        const double3 r = rvec(a.pos, b.x, b.y, W.box, W.hbox);
         const float2 p = a.bond_par[b.z];
-        const float rinv = rsqrtf(dist2f(r.x, r.y, r.z));
-        const float f = p.x * (p.y * rinv - 1.0f);
+        const double f = (double)p.x * ((double)p.y / sqrt(dot3(r, r)) - 1.0);
         add_force(a.facc, a.status, b.x, f * r.x, f * r.y, f * r.z);
         add_force(a.facc, a.status, b.y, -f * r.x, -f * r.y, -f * r.z);
         return;
@@ -142,19 +151,17 @@ __global__ void bonded_kernel(BondedArgs a) {
     if (idx < na) {  // angle_force_cuda.cu:19-52
         const int4 g = a.angles[idx];
         const WinDev W = a.win[a.atom_win[g.x]];
-        const float3 r1 = rvec(a.pos, g.x, g.y, W.box, W.hbox);
-        const float3 r2 = rvec(a.pos, g.y, g.z, W.box, W.hbox);
-        const float c11 = r1.x * r1.x + r1.y * r1.y + r1.z * r1.z;
-        const float c22 = r2.x * r2.x + r2.y * r2.y + r2.z * r2.z;
-        const float c12 = r1.x * r2.x + r1.y * r2.y + r1.z * r2.z;
-        const float b = -c12 / sqrtf(c11 * c22);
-        const float theta = b >= 1.0f ? 1.0e-16f : (b <= -1.0f ? kPi : acosf(b));
+        const double3 r1 = rvec(a.pos, g.x, g.y, W.box, W.hbox);
+        const double3 r2 = rvec(a.pos, g.y, g.z, W.box, W.hbox);
+        const double c11 = dot3(r1, r1), c22 = dot3(r2, r2), c12 = dot3(r1, r2);
+        const double b = -c12 / sqrt(c11 * c22);
+        const double theta = b >= 1.0 ? 1.0e-16 : (b <= -1.0 ? (double)kPi : acos(b));
         const float2 p = a.angle_par[g.w];
-        const float f = p.x * (theta - p.y) / sqrtf(c11 * c22 - c12 * c12);
-        const float a1 = c12 / c11, a2 = c12 / c22;
+        const double f = (double)p.x * (theta - (double)p.y) / sqrt(c11 * c22 - c12 * c12);
+        const double a1 = c12 / c11, a2 = c12 / c22;
         add_force(a.facc, a.status, g.x, f * (a1 * r1.x - r2.x), f * (a1 * r1.y - r2.y), f * (a1 * r1.z - r2.z));
-        add_force(a.facc, a.status, g.y, f * ((1.0f + a2) * r2.x - (1.0f + a1) * r1.x),
-                  f * ((1.0f + a2) * r2.y - (1.0f + a1) * r1.y), f * ((1.0f + a2) * r2.z - (1.0f + a1) * r1.z));
+        add_force(a.facc, a.status, g.y, f * ((1.0 + a2) * r2.x - (1.0 + a1) * r1.x),
+                  f * ((1.0 + a2) * r2.y - (1.0 + a1) * r1.y), f * ((1.0 + a2) * r2.z - (1.0 + a1) * r1.z));
         add_force(a.facc, a.status, g.z, f * (r1.x - a2 * r2.x), f * (r1.y - a2 * r2.y), f * (r1.z - a2 * r2.z));
         return;
     }
@@ -168,51 +175,47 @@ __global__ void bonded_kernel(BondedArgs a) {
         if (raw & 0x40000000) {  // scaled 1-4 when atoms.z > 0 && atoms.w > 0 (:60-82)
             const float2 ab = __ldg(a.ljab + a.atype[d.x].x * a.n_lj_types + a.atype[d.w].x);
             const float2 sc = a.sc14[ty];
-            const float3 r14 = rvec(a.pos, d.x, d.w, L, h);
-            const float rm = r14.x * r14.x + r14.y * r14.y + r14.z * r14.z;
-            const float r6 = 1.0f / (rm * rm * rm);
-            const float fe = a.pos[d.x].w * a.pos[d.w].w / (rm * sqrtf(rm) * sc.x);
-            const float fv = r6 * (12.0f * ab.x * r6 - 6.0f * ab.y) / (sc.y * rm);
-            const float f = fe + fv;
+            const double3 r14 = rvec(a.pos, d.x, d.w, L, h);
+            const double rm = dot3(r14, r14);
+            const double r6 = 1.0 / (rm * rm * rm);
+            const double fe = (double)a.pos[d.x].w * (double)a.pos[d.w].w / (rm * sqrt(rm) * (double)sc.x);
+            const double fv = r6 * (12.0 * (double)ab.x * r6 - 6.0 * (double)ab.y) / ((double)sc.y * rm);
+            const double f = fe + fv;
             add_force(a.facc, a.status, d.x, f * r14.x, f * r14.y, f * r14.z);
             add_force(a.facc, a.status, d.w, -f * r14.x, -f * r14.y, -f * r14.z);
         }
-        const float3 r12 = rvec(a.pos, d.x, d.y, L, h);
-        const float3 r23 = rvec(a.pos, d.y, d.z, L, h);
-        const float3 r34 = rvec(a.pos, d.z, d.w, L, h);
-        const float c11 = r12.x * r12.x + r12.y * r12.y + r12.z * r12.z;
-        const float c22 = r23.x * r23.x + r23.y * r23.y + r23.z * r23.z;
-        const float c12 = r12.x * r23.x + r12.y * r23.y + r12.z * r23.z;
-        const float c33 = r34.x * r34.x + r34.y * r34.y + r34.z * r34.z;
-        const float c23 = r23.x * r34.x + r23.y * r34.y + r23.z * r34.z;
-        const float c13 = r12.x * r34.x + r12.y * r34.y + r12.z * r34.z;
-        const float t1 = c13 * c22 - c12 * c23;
-        const float t2 = c11 * c23 - c12 * c13;
-        const float t3 = c12 * c12 - c11 * c22;
-        const float t4 = c22 * c33 - c23 * c23;
-        const float t5 = c13 * c23 - c12 * c33;
-        const float t6 = -t1;
-        const float b = sqrtf(-t3 * t4);
-        const float cs = t6 / b;
-        float fd = 0.0f;
-        if (cs > -1.0f && cs < 1.0f) {
-            const float phi = acosf(cs);
+        const double3 r12 = rvec(a.pos, d.x, d.y, L, h);
+        const double3 r23 = rvec(a.pos, d.y, d.z, L, h);
+        const double3 r34 = rvec(a.pos, d.z, d.w, L, h);
+        const double c11 = dot3(r12, r12), c22 = dot3(r23, r23), c12 = dot3(r12, r23);
+        const double c33 = dot3(r34, r34), c23 = dot3(r23, r34), c13 = dot3(r12, r34);
+        const double t1 = c13 * c22 - c12 * c23;
+        const double t2 = c11 * c23 - c12 * c13;
+        const double t3 = c12 * c12 - c11 * c22;
+        const double t4 = c22 * c33 - c23 * c23;
+        const double t5 = c13 * c23 - c12 * c33;
+        const double t6 = -t1;
+        const double b = sqrt(-t3 * t4);
+        const double cs = t6 / b;
+        double fd = 0.0;
+        if (cs > -1.0 && cs < 1.0) {
+            const double phi = acos(cs);
             const float4 p = a.dih_par[ty];
-            fd = p.x * p.y * sinf(p.x * phi - p.z) * c22 / (sinf(phi) * b);
+            fd = (double)p.x * (double)p.y * sin((double)p.x * phi - (double)p.z) * c22 / (sin(phi) * b);
         }
-        const float g1 = fd / t3, g4 = -fd / t4;
-        const float f1x = g1 * (t1 * r12.x + t2 * r23.x + t3 * r34.x);
-        const float f1y = g1 * (t1 * r12.y + t2 * r23.y + t3 * r34.y);
-        const float f1z = g1 * (t1 * r12.z + t2 * r23.z + t3 * r34.z);
-        const float f4x = g4 * (t4 * r12.x + t5 * r23.x + t6 * r34.x);
-        const float f4y = g4 * (t4 * r12.y + t5 * r23.y + t6 * r34.y);
-        const float f4z = g4 * (t4 * r12.z + t5 * r23.z + t6 * r34.z);
-        const float u = c12 / c22, v = c23 / c22;
+        const double g1 = fd / t3, g4 = -fd / t4;
+        const double f1x = g1 * (t1 * r12.x + t2 * r23.x + t3 * r34.x);
+        const double f1y = g1 * (t1 * r12.y + t2 * r23.y + t3 * r34.y);
+        const double f1z = g1 * (t1 * r12.z + t2 * r23.z + t3 * r34.z);
+        const double f4x = g4 * (t4 * r12.x + t5 * r23.x + t6 * r34.x);
+        const double f4y = g4 * (t4 * r12.y + t5 * r23.y + t6 * r34.y);
+        const double f4z = g4 * (t4 * r12.z + t5 * r23.z + t6 * r34.z);
+        const double u = c12 / c22, v = c23 / c22;
         add_force(a.facc, a.status, d.x, f1x, f1y, f1z);
-        add_force(a.facc, a.status, d.y, -(1.0f + u) * f1x + v * f4x, -(1.0f + u) * f1y + v * f4y,
-                  -(1.0f + u) * f1z + v * f4z);
-        add_force(a.facc, a.status, d.z, u * f1x - (1.0f + v) * f4x, u * f1y - (1.0f + v) * f4y,
-                  u * f1z - (1.0f + v) * f4z);
+        add_force(a.facc, a.status, d.y, -(1.0 + u) * f1x + v * f4x, -(1.0 + u) * f1y + v * f4y,
+                  -(1.0 + u) * f1z + v * f4z);
+        add_force(a.facc, a.status, d.z, u * f1x - (1.0 + v) * f4x, u * f1y - (1.0 + v) * f4y,
+                  u * f1z - (1.0 + v) * f4z);
         add_force(a.facc, a.status, d.w, f4x, f4y, f4z);
     }
 }
@@ -263,7 +266,7 @@ __global__ void __launch_bounds__(kUsThreads) umbrella_kernel(UmbrellaArgs a) {
         const int2 e = a.bias[W.bias_off + b];
         const double ku = e.y == 0 ? -(double)W.us_k : (double)W.us_k;  // us_class.cpp:153-154
         const double pf = ku * s_f[3] * (double)a.mfrac[W.bias_off + b];
-        add_force(a.facc, a.status, e.x, (float)(pf * s_f[0]), (float)(pf * s_f[1]), (float)(pf * s_f[2]));
+        add_force(a.facc, a.status, e.x, pf * s_f[0], pf * s_f[1], pf * s_f[2]);
     }
 }
 

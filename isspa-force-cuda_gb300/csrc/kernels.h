@@ -142,5 +142,9 @@ double measure_fp32_peak_tflops();
 int field_block_threads();
 int force_block_threads();
 int nonbond_block_threads();
+// launch-shape helpers for the work-list builder
+int field_points_per_block(int split);
+int field_blocks_per_sm(int split);
+int force_blocks_per_sm();
 
 }  // namespace isspa

@@ -45,6 +45,14 @@ class Engine:
         L.isspa_engine_info(h, C.byref(nw), C.byref(na), C.byref(npt))
         self.n_windows, self.n_atoms, self.n_points = nw.value, na.value, npt.value
 
+    def shapes(self) -> dict:
+        """Launch shapes chosen for the work lists (recorded with every benchmark)."""
+        v = (C.c_int * 7)()
+        abi.check(abi.lib().isspa_engine_shapes(self._h, v), "shapes")
+        keys = ("field_split", "field_tiles", "force_chunk", "force_items", "nonbond_items",
+                "nonbond_partners_per_item", "sms")
+        return dict(zip(keys, list(v)))
+
     # -------------------------------------------------------------- lifetime
     def close(self):
         if getattr(self, "_h", None):
