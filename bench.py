@@ -157,7 +157,8 @@ def run_gb300(args):
     N, M = sysm.n_atoms, sysm.n_mc
     P = N * M
     eng = ig.Engine(sysm)
-    shapes = eng.shapes()
+    shapes = eng.shapes() if args.no_autotune else eng.autotune()
+    shapes["autotuned"] = not args.no_autotune
     eng.step(args.warmup)
     eng.time_steps_detailed(max(args.warmup, 3), L2_FLUSH)
     eng.synchronize()
@@ -251,6 +252,7 @@ def run_batched(ig, args, plain_value):
     """64 umbrella windows (44..1100 atoms) in one engine vs the plain per-window path."""
     wins = ig.synth.config_batched(n_windows=64, seed=4)
     eng = ig.Engine(wins)
+    shapes = eng.shapes() if args.no_autotune else eng.autotune()
     nat = sum(w.n_atoms for w in wins)
     steps = max(3, args.steps // 10)
     eng.step(3)
@@ -268,7 +270,9 @@ def run_batched(ig, args, plain_value):
     eng.close()
     return {"windows": len(wins), "atoms_total": nat, "steps": steps,
             "value": round(batched, 1), "unit": UNIT, "ms_per_step": round(ms / steps, 4),
-            "plain_per_window_value": round(plain, 1), "speedup_vs_plain": round(batched / plain, 2)}
+            "plain_per_window_value": round(plain, 1), "speedup_vs_plain": round(batched / plain, 2),
+            "launch_shapes": shapes,
+            "kernel_ms_per_step": {k: round(v[0] / max(v[1], 1), 4) for k, v in kern.items()}}
 
 
 def run_reference(args):
@@ -321,6 +325,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank = int(os.environ.get("RANK", "0"))

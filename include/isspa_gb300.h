@@ -160,6 +160,12 @@ int isspa_engine_info(const isspa_engine *e, int *n_windows, int *n_atoms_total,
  * item, [3] force work items, [4] nonbond work items, [5] nonbond partners per
  * item, [6] SM count used for the choice. */
 int isspa_engine_shapes(const isspa_engine *e, int shape[7]);
+/* Autotuner: times every field-pass atom split and a set of force-pass chunk
+ * lengths (those filling 1..6 whole waves of resident blocks, and powers of
+ * two) on this engine's own workload with CUDA events (reps launches each),
+ * keeps the fastest of each and reports the result as isspa_engine_shapes
+ * does.  Clears the force accumulator; invalidates captured graphs. */
+int isspa_autotune(isspa_engine *e, int reps, int shape[7]);
 
 /* ---- per-step force calls (reference names and order) -------------------- */
 /* Each call adds its forces into the engine's force accumulator, exactly as the

@@ -40,11 +40,21 @@ struct WinDev {
 };
 
 // Packed per-point results of the field pass, consumed by the force pass.
+// With a_1 = p0<P1> w/n, a_2 = q0<P2> w/n, a_3 = o0<P3> w/n (the reference's
+// dipole / quadrupole / octupole amplitudes over rho, isspa_force_cuda.cu:
+// 279-287) the force of point p on atom i, per unit -q_i vtot_i, is
+//   r ri^5 [3 (D.r) + w g (7.5 a2 + 17.5 a3 g) - 1.5 a2 - 7.5 a3 g]
+//   - E^ ri^3 [g (3 a2 + 7.5 a3 g) - 1.5 a3 ri^2] - D ri^3,
+// w = E^.r, g = w ri^2, with the dipole vector D = a1 E^ inside rmax of the
+// atom's type and D = a1 E^ + p0 E0/(3n) outside: the constant-density
+// dielectric term (:306-312) is a dipole field of moment p0 E0/(3n) and folds
+// into the multipole's dipole term.
 struct PointsDev {
-    float4 *pos_s;   // x, y, z, w/n   (density per unit vtot)
-    float4 *ehat;    // unit mean field, 1/n
-    float4 *amp;     // p0<P1> w/n, q0<P2> w/n, o0<P3> w/n, 0
-    float4 *e0;      // E0/3 / n, 0
+    float4 *q0;   // x, y, z, w/n                 (position, density per unit vtot)
+    float4 *q1;   // E^x, E^y, E^z, 1.5 a2
+    float4 *q2;   // 7.5 a2, 17.5 a3, 3 a2, 7.5 a3
+    float4 *q3;   // D (inside rmax), 1.5 a3
+    float4 *q4;   // D (outside rmax), 1.5 a3
 };
 
 // Minimum image at most one box away (the reference's min_image): identical

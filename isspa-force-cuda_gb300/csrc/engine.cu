@@ -117,6 +117,97 @@ struct isspa_engine {
         if (!v.empty()) ck(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
         return p;
     }
+    template <typename T>
+    void release(T *&p) {
+        if (!p) return;
+        auto it = std::find(allocs.begin(), allocs.end(), (void *)p);
+        if (it != allocs.end()) allocs.erase(it);
+        cudaFree(p);
+        p = nullptr;
+    }
+
+    // ------------------------------------------------------- work lists
+    // Windows in descending size, so the costliest tiles are scheduled first.
+    std::vector<int> order;
+
+    static double wave_eff(long long units, long long slots) {
+        if (slots <= 0 || units <= 0) return 0.0;
+        const double waves = (double)units / (double)slots;
+        return waves / std::ceil(waves);
+    }
+    long long field_tiles_for(int S) const {
+        const int tp = field_points_per_block(S);
+        long long n = 0;
+        for (const WinDev &d : win_h) n += ((long long)d.n_atoms * n_mc + tp - 1) / tp;
+        return n;
+    }
+    long long force_items_for(long long C) const {
+        long long n = 0;
+        for (const WinDev &d : win_h) n += ((d.n_atoms + 127) / 128) * (((long long)d.n_atoms * n_mc + C - 1) / C);
+        return n;
+    }
+    // Grids of equal-work blocks should fill whole waves of resident blocks:
+    // the last, partial wave idles the remaining SMs.
+    int default_field_split() const {
+        int S = 4;
+        double best = -1.0;
+        for (int cand : {1, 2, 4, 8, 16}) {
+            const double e = wave_eff(field_tiles_for(cand), (long long)n_sms * field_blocks_per_sm(cand));
+            if (e > best + 0.02) {
+                best = e;
+                S = cand;
+            }
+        }
+        return S;
+    }
+    int default_force_chunk() const {
+        const long long slots = (long long)n_sms * std::max(1, force_blocks_per_sm());
+        double best = -1.0;
+        int C = 64;
+        for (long long c = 8192; c >= 64; --c) {  // longest chunk (fewest atomics) at equal efficiency
+            const long long n = force_items_for(c);
+            const double e = n < slots ? 0.5 * (double)n / (double)slots : wave_eff(n, slots);
+            if (e > best + 0.005) {
+                best = e;
+                C = (int)c;
+            }
+        }
+        return C;
+    }
+    void set_field_split(int S) {
+        std::vector<int4> t;
+        const int tp = field_points_per_block(S);
+        for (int w : order) {
+            const long long P = (long long)win_h[w].n_atoms * n_mc;
+            for (long long p = 0; p < P; p += tp)
+                t.push_back(make_int4(w, (int)(win_h[w].point_off + p), (int)std::min<long long>(tp, P - p), 0));
+        }
+        release(field_tiles);
+        field_tiles = upload(t);
+        n_field_tiles = (int)t.size();
+        field_split = S;
+    }
+    void set_force_chunk(int C) {
+        std::vector<int4> items;
+        std::vector<int2> chunks;
+        for (int w : order) {
+            const WinDev &d = win_h[w];
+            const long long P = (long long)d.n_atoms * n_mc;
+            const int c0 = (int)chunks.size();
+            for (long long p = 0; p < P; p += C)
+                chunks.push_back(make_int2((int)(d.point_off + p), (int)std::min<long long>(C, P - p)));
+            const int nc = (int)chunks.size() - c0;
+            for (int a = 0; a < d.n_atoms; a += 128)
+                for (int c = 0; c < nc; ++c)
+                    items.push_back(make_int4(w, d.atom_off + a, std::min(128, d.n_atoms - a), c0 + c));
+        }
+        release(force_items);
+        release(force_chunks);
+        force_items = upload(items);
+        force_chunks = upload(chunks);
+        n_force_items = (int)items.size();
+        force_chunk = C;
+    }
 
     ~isspa_engine() {
         if (stream) cudaStreamSynchronize(stream);
@@ -159,6 +250,7 @@ struct isspa_engine {
         a.out = pts;
         a.raw_e = raw_e;
         a.raw_e0 = raw_e0;
+        a.terms = opt.isspa_terms;
         a.status = status;
         return a;
     }
@@ -544,90 +636,26 @@ void build(isspa_engine &E, const std::vector<isspa_host_system> &ws) {
     }
 
     // ---- work lists ----
-    std::vector<int> order(W);
-    for (int w = 0; w < W; ++w) order[w] = w;
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return ws[a].n_atoms > ws[b].n_atoms; });
-    // field tiles: S warps split the atom loop of 128/S points
-    // Launch shapes are chosen so that grids fill whole waves of resident
-    // blocks (the tail wave of an equal-work grid idles the other SMs).
+    E.order.resize(W);
+    for (int w = 0; w < W; ++w) E.order[w] = w;
+    std::stable_sort(E.order.begin(), E.order.end(),
+                     [&](int a, int b) { return ws[a].n_atoms > ws[b].n_atoms; });
+    if (E.n_points > INT32_MAX) throw Fail{ISSPA_ERR_UNSUPPORTED};
     int dev = 0, sms = 0;
     ck(cudaGetDevice(&dev));
     ck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    auto wave_eff = [](long long units, long long slots) {
-        if (slots <= 0) return 0.0;
-        const double waves = (double)units / (double)slots;
-        return waves / std::ceil(waves);
-    };
-    auto tiles_for = [&](int S) {
-        const int tp = field_points_per_block(S);
-        long long n = 0;
-        for (int w = 0; w < W; ++w) n += ((long long)ws[w].n_atoms * E.n_mc + tp - 1) / tp;
-        return n;
-    };
+    E.n_sms = sms;
     int S = E.opt.field_split;
-    if (S != 1 && S != 2 && S != 4 && S != 8 && S != 16) {
-        double best = -1.0;
-        for (int cand : {1, 2, 4, 8, 16}) {
-            const double e = wave_eff(tiles_for(cand), (long long)sms * field_blocks_per_sm(cand));
-            if (e > best + 0.02) {
-                best = e;
-                S = cand;
-            }
-        }
-    }
-    E.field_split = S;
-    std::vector<int4> ftiles;
-    const int tp = field_points_per_block(S);
-    for (int w : order) {
-        long long P = (long long)ws[w].n_atoms * E.n_mc;
-        for (long long p = 0; p < P; p += tp)
-            ftiles.push_back(make_int4(w, (int)(E.win_h[w].point_off + p), (int)std::min<long long>(tp, P - p), 0));
-    }
-    if (E.n_points > INT32_MAX) throw Fail{ISSPA_ERR_UNSUPPORTED};
-    E.n_field_tiles = (int)ftiles.size();
-    // force items: 128-atom tiles x point chunks of C points
-    auto items_for = [&](long long C) {
-        long long n = 0;
-        for (int w = 0; w < W; ++w)
-            n += ((ws[w].n_atoms + 127) / 128) * (((long long)ws[w].n_atoms * E.n_mc + C - 1) / C);
-        return n;
-    };
-    int C = E.opt.force_chunk;
-    if (C <= 0) {
-        const long long fslots = (long long)sms * std::max(1, force_blocks_per_sm());
-        double best = -1.0;
-        C = 64;
-        for (long long c = 8192; c >= 64; c -= 32) {  // prefer long chunks (fewer atomics) at equal efficiency
-            const long long n = items_for(c);
-            const double e = n < fslots ? 0.5 * (double)n / (double)fslots : wave_eff(n, fslots);
-            if (e > best + 0.01) {
-                best = e;
-                C = (int)c;
-            }
-        }
-    }
-    E.force_chunk = C;
-    std::vector<int4> fitems;
-    std::vector<int2> fchunks;
-    for (int w : order) {
-        const WinDev &d = E.win_h[w];
-        long long P = (long long)d.n_atoms * E.n_mc;
-        int c0 = (int)fchunks.size();
-        for (long long p = 0; p < P; p += C)
-            fchunks.push_back(make_int2((int)(d.point_off + p), (int)std::min<long long>(C, P - p)));
-        int nc = (int)fchunks.size() - c0;
-        for (int a = 0; a < d.n_atoms; a += 128)
-            for (int c = 0; c < nc; ++c)
-                fitems.push_back(make_int4(w, d.atom_off + a, std::min(128, d.n_atoms - a), c0 + c));
-    }
-    E.n_force_items = (int)fitems.size();
+    if (S != 1 && S != 2 && S != 4 && S != 8 && S != 16) S = E.default_field_split();
+    E.set_field_split(S);
+    E.set_force_chunk(E.opt.force_chunk > 0 ? E.opt.force_chunk : E.default_force_chunk());
     // nonbond items: 128 i-atoms x J partners
     std::vector<int4> nitems;
     std::vector<int> nnj;
     long long npairs = 0;
     for (int w = 0; w < W; ++w) npairs += (long long)ws[w].n_atoms * ws[w].n_atoms;
     int J = (int)std::max<long long>(128, std::min<long long>(4096, ((npairs / (128LL * 608) + 127) / 128) * 128));
-    for (int w : order) {
+    for (int w : E.order) {
         const WinDev &d = E.win_h[w];
         for (int a = 0; a < d.n_atoms; a += 128)
             for (int j = 0; j < d.n_atoms; j += J) {
@@ -637,7 +665,6 @@ void build(isspa_engine &E, const std::vector<isspa_host_system> &ws) {
     }
     E.n_nb_items = (int)nitems.size();
     E.nb_chunk = J;
-    E.n_sms = sms;
 
     // ---- upload ----
     E.pos = E.upload(pos);
@@ -656,9 +683,6 @@ void build(isspa_engine &E, const std::vector<isspa_host_system> &ws) {
     E.ljab = E.upload(ljab);
     E.excl_start = E.upload(ex_start);
     E.excl = E.upload(ex_flat);
-    E.field_tiles = E.upload(ftiles);
-    E.force_items = E.upload(fitems);
-    E.force_chunks = E.upload(fchunks);
     E.nb_items = E.upload(nitems);
     E.nb_nj = E.upload(nnj);
     E.bonds = E.upload(bonds);
@@ -676,10 +700,11 @@ void build(isspa_engine &E, const std::vector<isspa_host_system> &ws) {
     E.cv = E.alloc<double>(W);
     ck(cudaMemset(E.com, 0, sizeof(double) * 6 * W));
     ck(cudaMemset(E.cv, 0, sizeof(double) * W));
-    E.pts.pos_s = E.alloc<float4>(E.n_points);
-    E.pts.ehat = E.alloc<float4>(E.n_points);
-    E.pts.amp = E.alloc<float4>(E.n_points);
-    E.pts.e0 = E.alloc<float4>(E.n_points);
+    E.pts.q0 = E.alloc<float4>(E.n_points);
+    E.pts.q1 = E.alloc<float4>(E.n_points);
+    E.pts.q2 = E.alloc<float4>(E.n_points);
+    E.pts.q3 = E.alloc<float4>(E.n_points);
+    E.pts.q4 = E.alloc<float4>(E.n_points);
     E.status = E.alloc<int>(1);
     E.d_step = E.alloc<uint32_t>(1);
     E.d_done = E.alloc<unsigned int>(1);
@@ -827,6 +852,71 @@ int isspa_engine_shapes(const isspa_engine *e, int shape[7]) {
     shape[5] = e->nb_chunk;
     shape[6] = e->n_sms;
     return ISSPA_OK;
+}
+
+int isspa_autotune(isspa_engine *e, int reps, int shape[7]) {
+    int rc = guard(e);
+    if (rc) return rc;
+    if (reps <= 0) reps = 3;
+    rc = run_guarded([&] {
+        auto time_it = [&](auto &&launch) {
+            launch();  // warm-up
+            ck(cudaEventRecord(e->ev_a, e->stream));
+            for (int r = 0; r < reps; ++r) launch();
+            ck(cudaEventRecord(e->ev_b, e->stream));
+            ck(cudaEventSynchronize(e->ev_b));
+            float ms = 0.f;
+            ck(cudaEventElapsedTime(&ms, e->ev_a, e->ev_b));
+            return ms / reps;
+        };
+        // field pass: every atom-loop split
+        float best = 1e30f;
+        int bestS = e->field_split;
+        for (int S : {1, 2, 4, 8, 16}) {
+            e->set_field_split(S);
+            const float ms = time_it([&] { launch_field(e->field_args(), S, false, e->stream); });
+            if (ms < best) {
+                best = ms;
+                bestS = S;
+            }
+        }
+        e->set_field_split(bestS);
+        launch_field(e->field_args(), bestS, false, e->stream);
+        // force pass: chunk lengths that fill 1..6 whole waves, and powers of two
+        const long long slots = (long long)e->n_sms * std::max(1, force_blocks_per_sm());
+        long long maxP = 0;
+        for (const WinDev &d : e->win_h) maxP = std::max(maxP, (long long)d.n_atoms * e->n_mc);
+        std::vector<int> cands = {e->default_force_chunk()};
+        for (int k = 1; k <= 6; ++k) {
+            long long lo = 64, hi = std::max<long long>(64, std::min<long long>(8192, maxP));
+            while (lo < hi) {  // smallest C with items <= k * slots
+                const long long mid = (lo + hi) / 2;
+                if (e->force_items_for(mid) <= k * slots) hi = mid;
+                else lo = mid + 1;
+            }
+            cands.push_back((int)lo);
+        }
+        for (int c : {128, 256, 512, 1024, 2048, 4096})
+            if (c <= std::max<long long>(128, maxP)) cands.push_back(c);
+        std::sort(cands.begin(), cands.end());
+        cands.erase(std::unique(cands.begin(), cands.end()), cands.end());
+        best = 1e30f;
+        int bestC = e->force_chunk;
+        for (int c : cands) {
+            e->set_force_chunk(c);
+            const float ms = time_it([&] { launch_force(e->force_args(), e->stream); });
+            if (ms < best) {
+                best = ms;
+                bestC = c;
+            }
+        }
+        e->set_force_chunk(bestC);
+        ck(cudaMemsetAsync(e->facc, 0, 3 * sizeof(unsigned long long) * e->n_atoms, e->stream));
+        ck(cudaStreamSynchronize(e->stream));
+        e->invalidate_graphs();
+    });
+    if (rc) return rc;
+    return shape ? isspa_engine_shapes(e, shape) : ISSPA_OK;
 }
 
 int isspa_zero_forces(isspa_engine *e) {
@@ -1089,7 +1179,7 @@ int isspa_get_point_fields(isspa_engine *e, float *xyz, float *w, int *n, float 
         std::vector<float4> a(e->n_points), b(e->n_points), c(e->n_points);
         ck(cudaMemcpyAsync(a.data(), e->raw_e, sizeof(float4) * np, cudaMemcpyDeviceToHost, e->stream));
         ck(cudaMemcpyAsync(b.data(), e->raw_e0, sizeof(float4) * np, cudaMemcpyDeviceToHost, e->stream));
-        ck(cudaMemcpyAsync(c.data(), e->pts.pos_s, sizeof(float4) * np, cudaMemcpyDeviceToHost, e->stream));
+        ck(cudaMemcpyAsync(c.data(), e->pts.q0, sizeof(float4) * np, cudaMemcpyDeviceToHost, e->stream));
         ck(cudaStreamSynchronize(e->stream));
         for (long long p = 0; p < np; ++p) {
             if (xyz) { xyz[3 * p] = c[p].x; xyz[3 * p + 1] = c[p].y; xyz[3 * p + 2] = c[p].z; }

@@ -16,8 +16,6 @@
 
 namespace {
 
-constexpr float kPiF = 3.1415926535f;  // constants.h:6
-
 struct LineFile {
     FILE *f = nullptr;
     explicit LineFile(const char *path) : f(std::fopen(path, "r")) {}

@@ -81,8 +81,7 @@ __device__ __forceinline__ void mc_point(uint32_t p, uint32_t window, uint32_t s
 // of 32 points; 4 warps per block up to S = 4, then 32*S threads.
 template <int S>
 struct FieldShape {
-    static constexpr int kThreads = S >= 4 ? 32 * S : kFieldThreads;
-    static constexpr int kGroups = kThreads / (32 * S);  // groups of 32 points per block
+    static constexpr int kThreads = S >= 4 ? 32 * S : kFieldThreads;  // kThreads/(32 S) point groups
 };
 
 template <int S, bool GEN, bool RAW>
@@ -215,16 +214,26 @@ __global__ void __launch_bounds__(FieldShape<S>::kThreads) field_kernel(FieldArg
     const float im = mag > 0.0f ? 1.0f / mag : 0.0f;
     float p1, p2, p3;
     langevin3(mag, p1, p2, p3);
-    const float third_n = inv_n * (1.0f / 3.0f);
-    a.out.pos_s[pg] = make_float4(px, py, pz, sden);
-    a.out.ehat[pg] = make_float4(ex * im, ey * im, ez * im, inv_n);
-    a.out.amp[pg] = make_float4(kP0 * p1 * sden, kQ0 * p2 * sden, kO0 * p3 * sden, 0.0f);
-    a.out.e0[pg] = make_float4(fx * third_n, fy * third_n, fz * third_n, 0.0f);
+    // term masks act here: a zero amplitude or far dipole removes a term exactly
+    const bool mp = a.terms & 1, cdd = a.terms & 4;
+    const float a1 = mp ? kP0 * p1 * sden : 0.0f;
+    const float a2 = mp ? kQ0 * p2 * sden : 0.0f;
+    const float a3 = mp ? kO0 * p3 * sden : 0.0f;
+    const float hx = ex * im, hy = ey * im, hz = ez * im;
+    const float cd = cdd ? kP0 * inv_n * (1.0f / 3.0f) : 0.0f;  // p0 E0 / (3 n)
+    a.out.q0[pg] = make_float4(px, py, pz, sden);
+    a.out.q1[pg] = make_float4(hx, hy, hz, 1.5f * a2);
+    a.out.q2[pg] = make_float4(7.5f * a2, 17.5f * a3, 3.0f * a2, 7.5f * a3);
+    a.out.q3[pg] = make_float4(a1 * hx, a1 * hy, a1 * hz, 1.5f * a3);
+    a.out.q4[pg] = make_float4(fmaf(a1, hx, cd * fx), fmaf(a1, hy, cd * fy), fmaf(a1, hz, cd * fz), 1.5f * a3);
 }
 
-template <int MASK>
-__global__ void __launch_bounds__(kForceThreads) force_kernel(ForceArgs a) {
-    __shared__ float4 s_p[kForceThreads], s_eh[kForceThreads], s_am[kForceThreads], s_e0[kForceThreads];
+// LJ = include the tabulated mean LJ force (term bit 2); the multipole and CDD
+// terms are shaped by the per-point constants of the field pass.
+template <bool LJ>
+__global__ void __launch_bounds__(kForceThreads, 10) force_kernel(ForceArgs a) {
+    __shared__ float4 s_q0[kForceThreads], s_q1[kForceThreads], s_q2[kForceThreads];
+    __shared__ float4 s_q3[kForceThreads], s_q4[kForceThreads];
     const int4 item = a.items[blockIdx.x];
     const WinDev W = a.win[item.x];
     const int2 ch = a.chunks[item.w];
@@ -236,7 +245,6 @@ __global__ void __launch_bounds__(kForceThreads) force_kernel(ForceArgs a) {
     const float rm = __ldg(a.rmax + ity);
     const float rm2 = __fmul_rn(rm, rm);
     const int frow = ity * a.n_f;
-    const int terms = MASK >= 0 ? MASK : a.terms;
     const float L = W.box, h = W.hbox;
     const float f_r0 = a.f_r0, f_dr = a.f_dr, f_inv = a.f_inv;
     const int nf = a.n_f;
@@ -248,64 +256,57 @@ __global__ void __launch_bounds__(kForceThreads) force_kernel(ForceArgs a) {
     long long fxa = 0, fya = 0, fza = 0;
 
     for (int p0 = 0; p0 < ch.y; p0 += kForceThreads) {
-        float qx = 0.f, qy = 0.f, qz = 0.f;  // terms proportional to -q_i vtot_i
-        float lx = 0.f, ly = 0.f, lz = 0.f;  // tabulated LJ, proportional to -vtot_i
+        float qx = 0.f, qy = 0.f, qz = 0.f;  // polarisation terms, per unit -q_i vtot_i
+        float lx = 0.f, ly = 0.f, lz = 0.f;  // tabulated LJ, per unit -vtot_i
         const int pn = min(kForceThreads, ch.y - p0);
         __syncthreads();
         if (t < pn) {
             const long long pg = (long long)ch.x + p0 + t;
-            s_p[t] = a.pts.pos_s[pg];
-            s_eh[t] = a.pts.ehat[pg];
-            s_am[t] = a.pts.amp[pg];
-            s_e0[t] = a.pts.e0[pg];
+            s_q0[t] = a.pts.q0[pg];
+            s_q1[t] = a.pts.q1[pg];
+            s_q2[t] = a.pts.q2[pg];
+            s_q3[t] = a.pts.q3[pg];
+            s_q4[t] = a.pts.q4[pg];
         }
         __syncthreads();
 #pragma unroll 2
         for (int k = 0; k < pn; ++k) {
-            const float4 P = s_p[k];
+            const float4 P = s_q0[k];
             const float rx = mimg(P.x - xi.x, L, h);
             const float ry = mimg(P.y - xi.y, L, h);
             const float rz = mimg(P.z - xi.z, L, h);
             const float d2 = dist2f(rx, ry, rz);
+            const bool inside = d2 <= rm2;  // (:291)
             const float ri = rsqrtf(d2);
             const float ri2 = ri * ri;
-            if (terms & 1) {  // dipole / quadrupole / octupole (:274-289)
-                const float4 E = s_eh[k];
-                const float4 A = s_am[k];
-                const float Rz = (E.x * rx + E.y * ry + E.z * rz) * ri;
-                const float Rz2 = Rz * Rz;
-                const float dp1 = 3.0f * Rz;
-                const float dp2 = fmaf(7.5f, Rz2, -1.5f);
-                const float dp3 = fmaf(17.5f, Rz2, -7.5f) * Rz;
-                const float t1 = A.x * ri2 * ri;
-                const float t2 = A.y * ri2 * ri2;
-                const float t3 = A.z * ri2 * ri2 * ri;
-                const float cR = fmaf(t1, dp1, fmaf(t2, dp2, t3 * dp3)) * ri;
-                const float cE = fmaf(t2, dp1, fmaf(t3, dp2, t1));
-                qx = fmaf(cR, rx, fmaf(-cE, E.x, qx));
-                qy = fmaf(cR, ry, fmaf(-cE, E.y, qy));
-                qz = fmaf(cR, rz, fmaf(-cE, E.z, qz));
-            }
-            if (d2 <= rm2) {
-                if (terms & 2) {  // tabulated mean LJ force (:291-305)
-                    const float dist = __fsqrt_rn(d2);
-                    const int bin = (int)__fmaf_rn(__fsub_rn(dist, f_r0), f_inv, 0.5f);
-                    if (bin >= 0 && bin < nf) {
-                        const float2 tv = __ldg(a.ftab + frow + bin);
-                        const float fr = (dist - fmaf((float)bin, f_dr, f_r0)) * f_inv;
-                        const float fv = fmaf(fr, tv.y - tv.x, tv.x) * P.w * ri;
-                        lx = fmaf(fv, rx, lx);
-                        ly = fmaf(fv, ry, ly);
-                        lz = fmaf(fv, rz, lz);
-                    }
+            const float ri3 = ri2 * ri;
+            const float ri5 = ri3 * ri2;
+            const float4 E = s_q1[k];
+            const float4 K = s_q2[k];
+            const float4 D = (inside ? s_q3 : s_q4)[k];
+            // multipole (:274-289) with the CDD term (:306-312) folded into D
+            const float w = fmaf(E.x, rx, fmaf(E.y, ry, E.z * rz));
+            const float dD = fmaf(D.x, rx, fmaf(D.y, ry, D.z * rz));
+            const float g = w * ri2;
+            float X = (w * g) * fmaf(K.y, g, K.x);
+            X = fmaf(3.0f, dD, X) - E.w;
+            X = fmaf(-K.w, g, X);
+            const float cR = X * ri5;
+            const float cE = fmaf(-D.w, ri2, fmaf(K.w, g, K.z) * g) * ri3;
+            qx = fmaf(cR, rx, fmaf(-cE, E.x, fmaf(-ri3, D.x, qx)));
+            qy = fmaf(cR, ry, fmaf(-cE, E.y, fmaf(-ri3, D.y, qy)));
+            qz = fmaf(cR, rz, fmaf(-cE, E.z, fmaf(-ri3, D.z, qz)));
+            if (LJ && inside) {  // tabulated mean LJ force (:291-305)
+                const float dist = __fsqrt_rn(d2);
+                const int bin = (int)__fmaf_rn(__fsub_rn(dist, f_r0), f_inv, 0.5f);
+                if (bin >= 0 && bin < nf) {
+                    const float2 tv = __ldg(a.ftab + frow + bin);
+                    const float fr = (dist - fmaf((float)bin, f_dr, f_r0)) * f_inv;
+                    const float fv = fmaf(fr, tv.y - tv.x, tv.x) * P.w * ri;
+                    lx = fmaf(fv, rx, lx);
+                    ly = fmaf(fv, ry, ly);
+                    lz = fmaf(fv, rz, lz);
                 }
-            } else if (terms & 4) {  // constant-density dielectric (:306-312)
-                const float4 E0 = s_e0[k];
-                const float tc = kP0 * ri2 * ri;
-                const float pd = 3.0f * (E0.x * rx + E0.y * ry + E0.z * rz) * ri2;
-                qx = fmaf(tc, fmaf(pd, rx, -E0.x), qx);
-                qy = fmaf(tc, fmaf(pd, ry, -E0.y), qy);
-                qz = fmaf(tc, fmaf(pd, rz, -E0.z), qz);
             }
         }
         const float Fx = -vt * fmaf(xi.w, qx, lx);
@@ -374,14 +375,14 @@ int field_blocks_per_sm(int split) {
 
 int force_blocks_per_sm() {
     int n = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, force_kernel<7>, kForceThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, force_kernel<true>, kForceThreads, 0);
     return n;
 }
 
 void launch_force(const ForceArgs &a, cudaStream_t s) {
     if (a.n_items <= 0) return;
-    if (a.terms == 7) force_kernel<7><<<a.n_items, kForceThreads, 0, s>>>(a);
-    else force_kernel<-1><<<a.n_items, kForceThreads, 0, s>>>(a);
+    if (a.terms & 2) force_kernel<true><<<a.n_items, kForceThreads, 0, s>>>(a);
+    else force_kernel<false><<<a.n_items, kForceThreads, 0, s>>>(a);
 }
 
 }  // namespace isspa

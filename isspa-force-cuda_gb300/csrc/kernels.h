@@ -26,6 +26,7 @@ struct FieldArgs {
     PointsDev out;
     float4 *raw_e;         // optional: E, w
     float4 *raw_e0;        // optional: E0, n
+    int terms;             // IS-SPA force terms: 1 multipole, 2 tabulated LJ, 4 CDD
     int *status;
 };
 

@@ -82,6 +82,7 @@ SIGNATURES = [
     ("isspa_engine_destroy", None, [_P]),
     ("isspa_engine_info", C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_longlong)]),
     ("isspa_engine_shapes", C.c_int, [_P, C.POINTER(C.c_int)]),
+    ("isspa_autotune", C.c_int, [_P, C.c_int, C.POINTER(C.c_int)]),
     ("isspa_zero_forces", C.c_int, [_P]),
     ("bond_force_cuda", C.c_int, [_P, _FP]),
     ("angle_force_cuda", C.c_int, [_P, _FP]),

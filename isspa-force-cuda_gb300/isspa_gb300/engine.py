@@ -53,6 +53,12 @@ class Engine:
                 "nonbond_partners_per_item", "sms")
         return dict(zip(keys, list(v)))
 
+    def autotune(self, reps: int = 3) -> dict:
+        """Time candidate launch shapes on this workload and keep the fastest."""
+        v = (C.c_int * 7)()
+        abi.check(abi.lib().isspa_autotune(self._h, int(reps), v), "autotune")
+        return self.shapes()
+
     # -------------------------------------------------------------- lifetime
     def close(self):
         if getattr(self, "_h", None):
