@@ -245,6 +245,38 @@ int isspa_cell_list(isspa_engine *e, float rc, const int ncell[3], int *cell_of_
  * GPU and returns the measured TFLOP/s (FMA = 2 flops). */
 int isspa_measure_fp32_peak(double *tflops);
 
+/* ---- IS-SPA force without any allocation ---------------------------------
+ * No counterpart in the reference.  For callers that must not call cudaMalloc
+ * (or any allocating routine): code running inside another framework's memory
+ * pool, a host process whose device memory is budgeted up front, or a real-time
+ * loop that may not take the allocator's locks.  All arrays below are DEVICE
+ * pointers owned by the caller; the per-point field records, packed tables and
+ * force accumulator live in one static device buffer of
+ * ISSPA_NOALLOC_SCRATCH_BYTES that every GPU loading this library holds until
+ * the process exits.  Systems whose working set does not fit are rejected with
+ * ISSPA_ERR_UNSUPPORTED (roughly 190 k MC points, e.g. 3800 atoms at nMC 50).
+ * The first call on a device looks up that buffer's device address (make it
+ * before any stream capture); calls share the buffer, so calls that overlap on
+ * the GPU (different streams, devices' own queues) race and must be ordered by
+ * the caller.  Computes the same IS-SPA force as isspa_force_cuda for one
+ * window and writes it to force_out ([n_atoms][4], .w = 0), on `stream`
+ * (a cudaStream_t; NULL = legacy default stream), without synchronising. */
+#define ISSPA_NOALLOC_SCRATCH_BYTES (16u << 20)
+typedef struct isspa_noalloc_inputs {
+    int n_atoms, n_mc, n_isspa_types;
+    const float *pos;         /* [n_atoms][4]: x, y, z, charge/sqrt(eps) */
+    const int *isspa_type;    /* [n_atoms] */
+    const float *rmax;        /* [n_isspa_types] */
+    int n_g, n_e, n_f;
+    const float *g_table, *e_table, *f_table; /* [n_isspa_types][n_g | n_e | n_f] */
+    float g_r0, g_dr, e_r0, e_dr, f_r0, f_dr;
+    float box;
+    uint64_t seed;
+    uint32_t step;            /* Philox step key of the MC points */
+    int terms;                /* 1 multipole, 2 tabulated LJ, 4 CDD; 0 => all */
+} isspa_noalloc_inputs;
+int isspa_force_noalloc(const isspa_noalloc_inputs *in, float *force_out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -62,6 +62,19 @@ class RunConfig(C.Structure):
                                          "cutoff")]
 
 
+class NoallocInputs(C.Structure):
+    """isspa_noalloc_inputs: device pointers owned by a caller that cannot allocate."""
+    _fields_ = [("n_atoms", C.c_int), ("n_mc", C.c_int), ("n_isspa_types", C.c_int),
+                ("pos", C.c_void_p), ("isspa_type", C.c_void_p), ("rmax", C.c_void_p),
+                ("n_g", C.c_int), ("n_e", C.c_int), ("n_f", C.c_int),
+                ("g_table", C.c_void_p), ("e_table", C.c_void_p), ("f_table", C.c_void_p),
+                ("g_r0", C.c_float), ("g_dr", C.c_float), ("e_r0", C.c_float), ("e_dr", C.c_float),
+                ("f_r0", C.c_float), ("f_dr", C.c_float), ("box", C.c_float),
+                ("seed", C.c_uint64), ("step", C.c_uint32), ("terms", C.c_int)]
+
+
+NOALLOC_SCRATCH_BYTES = 16 << 20
+
 # (name, restype, argtypes); every exported entry point of include/isspa_gb300.h
 _P = C.c_void_p
 _FP = C.POINTER(C.c_float)
@@ -114,6 +127,7 @@ SIGNATURES = [
     ("isspa_neighbor_list", C.c_int, [_P, C.c_float, C.c_int, _P, _P]),
     ("isspa_cell_list", C.c_int, [_P, C.c_float, _P, _P]),
     ("isspa_measure_fp32_peak", C.c_int, [C.POINTER(C.c_double)]),
+    ("isspa_force_noalloc", C.c_int, [C.POINTER(NoallocInputs), _P, _P]),
 ]
 
 _lib = None
