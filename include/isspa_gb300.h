@@ -232,6 +232,29 @@ int isspa_clear_mc_points(isspa_engine *e);
 int isspa_get_point_fields(isspa_engine *e, float *xyz, float *w, int *n, float *efield,
                            float *e0field, long long n_points_total);
 
+/* ---- force-field parameters and their gradient --------------------------- */
+/* Replaces the engine's tables (host arrays in the layouts of
+ * isspa_system_desc; NULL keeps a table): ISSPA_DENSITIES, ISSPA_EFIELD,
+ * ISSPA_FORCES, and the packed LJ A/B coefficients.  Shapes are unchanged. */
+int isspa_set_tables(isspa_engine *e, const float *g_table, const float *e_table, const float *f_table,
+                     const float *lj_ab);
+/* Mean COM-axis force of every restrained window and its gradient with
+ * respect to the force field (no counterpart in the reference, which has no
+ * derivatives).  For frame f the engine's positions are frames[f] ([Ntot][4];
+ * NULL = the current positions) and the MC points are regenerated from the
+ * Philox counters of steps[f] (no point storage).  With c_i = +n/2 on restraint
+ * group 0 and -n/2 on group 1 (n the unit vector between the group centres of
+ * mass, us_force_cuda.cu:30-34), J_w = mean_f sum_i c_i . F_i, F_i the total
+ * non-restraint force (bonded, IS-SPA, nonbond).  Outputs per window, FP64:
+ *   J [n_windows], dJ_df [n_windows][n_isspa_types*n_f] (ISSPA_FORCES entries),
+ *   dJ_dg [n_windows][n_isspa_types*n_g] (ISSPA_DENSITIES entries),
+ *   dJ_dA, dJ_dB [n_windows][n_lj_types*(n_lj_types+1)/2] (packed LJ A, B).
+ * Windows without a restraint get zeros.  The engine's positions and step
+ * counter are restored; the force accumulator is cleared.  Any output may be
+ * NULL. */
+int isspa_adjoint_mean_force(isspa_engine *e, int n_frames, const float *frames, const uint32_t *steps,
+                             double *J, double *dJ_df, double *dJ_dg, double *dJ_dA, double *dJ_dB);
+
 /* ---- neighbour and cell lists (neighborlist_cuda.cu, cell_list_cuda.cu) -- */
 /* All-pairs neighbour list of window 0 with r^2 < rnn^2, exclusions as the
  * nonbond kernel; rows sorted ascending.  rows [n_atoms][max_per_atom], counts

@@ -77,6 +77,15 @@ struct isspa_engine {
     int n_us = 0;
     int2 *bias = nullptr;
     float *mfrac = nullptr;
+    std::vector<int2> bias_h;
+    std::vector<float> mfrac_h, lj_ab_h, g_raw_h, e_raw_h, f_raw_h;
+    std::vector<int> nbp_h;
+    float *g_raw = nullptr;
+    int *nbp = nullptr;
+    // adjoint buffers (allocated on first use)
+    int *point_win = nullptr, *adj_off = nullptr, *adj_atoms = nullptr;
+    double *cvec = nullptr, *lam = nullptr, *grads = nullptr;
+    int n_adj_cap = 0;
     double *com = nullptr, *cv = nullptr;
     PointsDev pts{};
     float4 *raw_e = nullptr, *raw_e0 = nullptr;
@@ -479,6 +488,35 @@ bool same_force_field(const isspa_host_system &a, const isspa_host_system &b) {
            a.f_r0 == b.f_r0 && a.f_dr == b.f_dr && a.n_mc == b.n_mc && a.seed == b.seed;
 }
 
+// Packs the IS-SPA tables for the kernels: g/E as (v_b, v_b+1) pairs per bin of
+// the g grid, the force table as (f_k, f_k+1) pairs, both with the reference's
+// flat-row semantics (the upper neighbour of a row's last bin is the next
+// type's first entry, and zero past the last type).
+void pack_isspa_tables(int nt, int ng, int ne, int nf, const std::vector<float> &g, const std::vector<float> &e,
+                       const std::vector<float> &f, std::vector<float4> &gtab, std::vector<float2> &ftab) {
+    const int pad = std::max({ng, ne, nf}) + 1;
+    auto padded = [&](const std::vector<float> &t) {
+        std::vector<float> q(t);
+        q.resize(t.size() + pad, 0.f);
+        return q;
+    };
+    const std::vector<float> Gp = padded(g), Ep = padded(e), Fp = padded(f);
+    gtab.assign((size_t)nt * (ng - 1), make_float4(0.f, 0.f, 0.f, 0.f));
+    for (int t = 0; t < nt; ++t)
+        for (int b = 0; b < ng - 1; ++b) {
+            const size_t gi = (size_t)t * ng + b, ei = (size_t)t * ne + b;
+            gtab[(size_t)t * (ng - 1) + b] = make_float4(Gp[gi], Gp[gi + 1], Ep[ei], Ep[ei + 1]);
+        }
+    ftab.assign((size_t)nt * nf, make_float2(0.f, 0.f));
+    for (size_t fi = 0; fi < ftab.size(); ++fi) ftab[fi] = make_float2(Fp[fi], Fp[fi + 1]);
+}
+
+// LJ (A, B) for every ordered type pair, from the packed triangle.
+void expand_lj(int nlj, const std::vector<int> &nbp, const std::vector<float> &lj_ab, std::vector<float2> &ljab) {
+    ljab.resize((size_t)nlj * nlj);
+    for (int i = 0; i < nlj * nlj; ++i) ljab[i] = make_float2(lj_ab[2 * nbp[i]], lj_ab[2 * nbp[i] + 1]);
+}
+
 void build(isspa_engine &E, const std::vector<isspa_host_system> &ws) {
     const isspa_host_system &f0 = ws[0];
     const int W = (int)ws.size();
@@ -575,37 +613,17 @@ void build(isspa_engine &E, const std::vector<isspa_host_system> &ws) {
 
     // ---- force-field tables ----
     const int nt = E.n_itypes;
-    const int pad = std::max({f0.n_g, f0.n_e, f0.n_f}) + 1;
-    auto padded = [&](const std::vector<float> &t) {
-        std::vector<float> p(t);
-        p.resize(t.size() + pad, 0.f);
-        return p;
-    };
-    std::vector<float> Gp = padded(f0.g_table), Ep = padded(f0.e_table), Fp = padded(f0.f_table);
-    std::vector<float4> gtab((size_t)nt * (f0.n_g - 1));
-    for (int t = 0; t < nt; ++t)
-        for (int b = 0; b < f0.n_g - 1; ++b) {
-            size_t gi = (size_t)t * f0.n_g + b, ei = (size_t)t * f0.n_e + b;
-            gtab[(size_t)t * (f0.n_g - 1) + b] = make_float4(Gp[gi], Gp[gi + 1], Ep[ei], Ep[ei + 1]);
-        }
-    std::vector<float2> ftab((size_t)nt * f0.n_f);
-    for (int t = 0; t < nt; ++t)
-        for (int b = 0; b < f0.n_f; ++b) {
-            size_t fi = (size_t)t * f0.n_f + b;
-            ftab[fi] = make_float2(Fp[fi], Fp[fi + 1]);
-        }
+    std::vector<float4> gtab;
+    std::vector<float2> ftab;
+    pack_isspa_tables(nt, f0.n_g, f0.n_e, f0.n_f, f0.g_table, f0.e_table, f0.f_table, gtab, ftab);
     std::vector<float> vtot(nt);
     for (int t = 0; t < nt; ++t) {
         // isspa_class.cpp:41 (double arithmetic, stored as float)
         double r = f0.rmax[t];
         vtot[t] = (float)(4.0 / 3.0 * (double)kPi * r * r * r * 0.0074 / (double)(float)f0.n_mc);
     }
-    const int nlj = f0.n_lj_types;
-    std::vector<float2> ljab((size_t)nlj * nlj);
-    for (int i = 0; i < nlj * nlj; ++i) {
-        int k = f0.nb_parm_index[i];
-        ljab[i] = make_float2(f0.lj_ab[2 * k], f0.lj_ab[2 * k + 1]);
-    }
+    std::vector<float2> ljab;
+    expand_lj(f0.n_lj_types, f0.nb_parm_index, f0.lj_ab, ljab);
     std::vector<int> ex_start(E.n_atoms + 1, 0), ex_flat;
     for (int i = 0; i < E.n_atoms; ++i) {
         ex_start[i] = (int)ex_flat.size();
@@ -696,6 +714,16 @@ void build(isspa_engine &E, const std::vector<isspa_host_system> &ws) {
     E.us_windows = E.upload(us_windows);
     E.bias = E.upload(bias);
     E.mfrac = E.upload(mfrac);
+    // host copies kept for the adjoint and for table updates
+    E.bias_h = bias;
+    E.mfrac_h = mfrac;
+    E.nbp_h = f0.nb_parm_index;
+    E.lj_ab_h = f0.lj_ab;
+    E.g_raw_h = f0.g_table;
+    E.e_raw_h = f0.e_table;
+    E.f_raw_h = f0.f_table;
+    E.g_raw = E.upload(f0.g_table);
+    E.nbp = E.upload(f0.nb_parm_index);
     E.com = E.alloc<double>(6 * (size_t)W);
     E.cv = E.alloc<double>(W);
     ck(cudaMemset(E.com, 0, sizeof(double) * 6 * W));
@@ -852,6 +880,189 @@ int isspa_engine_shapes(const isspa_engine *e, int shape[7]) {
     shape[5] = e->nb_chunk;
     shape[6] = e->n_sms;
     return ISSPA_OK;
+}
+
+int isspa_set_tables(isspa_engine *e, const float *g_table, const float *e_table, const float *f_table,
+                     const float *lj_ab) {
+    int rc = guard(e);
+    if (rc) return rc;
+    return run_guarded([&] {
+        const int nt = e->n_itypes, nlj = e->n_lj_types;
+        if (g_table) e->g_raw_h.assign(g_table, g_table + (size_t)nt * e->n_g);
+        if (e_table) e->e_raw_h.assign(e_table, e_table + (size_t)nt * e->n_e);
+        if (f_table) e->f_raw_h.assign(f_table, f_table + (size_t)nt * e->n_f);
+        if (lj_ab) e->lj_ab_h.assign(lj_ab, lj_ab + (size_t)nlj * (nlj + 1));
+        for (float v : e->g_raw_h) if (!std::isfinite(v)) throw Fail{ISSPA_ERR_ARG};
+        for (float v : e->e_raw_h) if (!std::isfinite(v)) throw Fail{ISSPA_ERR_ARG};
+        for (float v : e->f_raw_h) if (!std::isfinite(v)) throw Fail{ISSPA_ERR_ARG};
+        for (float v : e->lj_ab_h) if (!std::isfinite(v)) throw Fail{ISSPA_ERR_ARG};
+        std::vector<float4> gtab;
+        std::vector<float2> ftab, ljab;
+        pack_isspa_tables(nt, e->n_g, e->n_e, e->n_f, e->g_raw_h, e->e_raw_h, e->f_raw_h, gtab, ftab);
+        expand_lj(nlj, e->nbp_h, e->lj_ab_h, ljab);
+        ck(cudaStreamSynchronize(e->stream));
+        ck(cudaMemcpy(e->gtab, gtab.data(), sizeof(float4) * gtab.size(), cudaMemcpyHostToDevice));
+        ck(cudaMemcpy(e->ftab, ftab.data(), sizeof(float2) * ftab.size(), cudaMemcpyHostToDevice));
+        ck(cudaMemcpy(e->ljab, ljab.data(), sizeof(float2) * ljab.size(), cudaMemcpyHostToDevice));
+        ck(cudaMemcpy(e->g_raw, e->g_raw_h.data(), sizeof(float) * e->g_raw_h.size(), cudaMemcpyHostToDevice));
+    });
+}
+
+int isspa_adjoint_mean_force(isspa_engine *e, int n_frames, const float *frames, const uint32_t *steps, double *J,
+                             double *dJ_df, double *dJ_dg, double *dJ_dA, double *dJ_dB) {
+    if (!e || n_frames <= 0 || !steps) return ISSPA_ERR_ARG;
+    int rc = guard(e);
+    if (rc) return rc;
+    const int W = e->n_windows, N = e->n_atoms;
+    const long long P = e->n_points;
+    const long long nF = (long long)e->n_itypes * e->n_f, nG = (long long)e->n_itypes * e->n_g;
+    const int ntt = e->n_lj_types * (e->n_lj_types + 1) / 2;
+    const long long per_w = nF + nG + 2LL * ntt;
+    std::vector<float4> saved(N);
+    uint32_t saved_step = 0;
+    rc = run_guarded([&] {
+        if (!e->raw_e) {
+            e->raw_e = e->alloc<float4>(P);
+            e->raw_e0 = e->alloc<float4>(P);
+        }
+        if (!e->point_win) {
+            std::vector<int> pw(P);
+            for (int w = 0; w < W; ++w)
+                for (long long p = 0; p < (long long)e->win_h[w].n_atoms * e->n_mc; ++p) pw[e->win_h[w].point_off + p] = w;
+            e->point_win = e->upload(pw);
+            e->cvec = e->alloc<double>(3 * (size_t)N);
+            e->lam = e->alloc<double>(P);
+            e->grads = e->alloc<double>((size_t)W * per_w);
+            e->adj_off = e->alloc<int>(W + 1);
+            e->adj_atoms = e->alloc<int>(std::max<size_t>(1, e->bias_h.size()));
+        }
+        ck(cudaMemcpy(saved.data(), e->pos, sizeof(float4) * N, cudaMemcpyDeviceToHost));
+        ck(cudaMemcpy(&saved_step, e->d_step, sizeof saved_step, cudaMemcpyDeviceToHost));
+        ck(cudaMemset(e->grads, 0, sizeof(double) * (size_t)W * per_w));
+        std::vector<double> Jw(W, 0.0), cvec(3 * (size_t)N), facc(3 * (size_t)N);
+        std::vector<long long> acc(3 * (size_t)N);
+        for (int f = 0; f < n_frames; ++f) {
+            const float4 *X = frames ? reinterpret_cast<const float4 *>(frames) + (size_t)f * N : saved.data();
+            if (frames) ck(cudaMemcpy(e->pos, X, sizeof(float4) * N, cudaMemcpyHostToDevice));
+            ck(cudaMemcpy(e->d_step, &steps[f], sizeof(uint32_t), cudaMemcpyHostToDevice));
+            // weights c_i = +-n/2 on the two restraint groups of each window
+            std::fill(cvec.begin(), cvec.end(), 0.0);
+            std::vector<int> off(W + 1, 0), atoms;
+            for (int w = 0; w < W; ++w) {
+                off[w] = (int)atoms.size();
+                const WinDev &d = e->win_h[w];
+                if (!d.us_on) continue;
+                double c[2][3] = {{0, 0, 0}, {0, 0, 0}};
+                for (int b = 0; b < d.n_bias; ++b) {
+                    const int2 bl = e->bias_h[d.bias_off + b];
+                    const double m = e->mfrac_h[d.bias_off + b];
+                    c[bl.y][0] += m * X[bl.x].x;
+                    c[bl.y][1] += m * X[bl.x].y;
+                    c[bl.y][2] += m * X[bl.x].z;
+                }
+                double n[3], nn = 0.0;
+                for (int k = 0; k < 3; ++k) {
+                    double v = c[0][k] - c[1][k];
+                    if (v > 0.5 * d.box) v -= d.box;
+                    else if (v < -0.5 * d.box) v += d.box;
+                    n[k] = v;
+                    nn += v * v;
+                }
+                nn = std::sqrt(nn);
+                for (int b = 0; b < d.n_bias; ++b) {
+                    const int2 bl = e->bias_h[d.bias_off + b];
+                    const double sgn = bl.y == 0 ? 0.5 : -0.5;
+                    for (int k = 0; k < 3; ++k) cvec[3 * (size_t)bl.x + k] += sgn * n[k] / nn;
+                    if (std::find(atoms.begin() + off[w], atoms.end(), bl.x) == atoms.end()) atoms.push_back(bl.x);
+                }
+            }
+            off[W] = (int)atoms.size();
+            ck(cudaMemcpy(e->cvec, cvec.data(), sizeof(double) * cvec.size(), cudaMemcpyHostToDevice));
+            ck(cudaMemcpy(e->adj_off, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice));
+            if (!atoms.empty())
+                ck(cudaMemcpy(e->adj_atoms, atoms.data(), sizeof(int) * atoms.size(), cudaMemcpyHostToDevice));
+            // the value: every non-restraint force of the frame, projected
+            ck(cudaMemsetAsync(e->facc, 0, 3 * sizeof(unsigned long long) * N, e->stream));
+            launch_bonded(e->bonded_args(1, 1, 1), e->stream);
+            launch_field(e->field_args(), e->field_split, true, e->stream);
+            launch_force(e->force_args(), e->stream);
+            launch_nonbond(e->nonbond_args(), e->stream);
+            ck(cudaGetLastError());
+            ck(cudaMemcpyAsync(acc.data(), e->facc, sizeof(long long) * acc.size(), cudaMemcpyDeviceToHost, e->stream));
+            ck(cudaStreamSynchronize(e->stream));
+            for (int w = 0; w < W; ++w) {
+                const WinDev &d = e->win_h[w];
+                for (int i = d.atom_off; i < d.atom_off + d.n_atoms; ++i)
+                    for (int k = 0; k < 3; ++k) Jw[w] += cvec[3 * (size_t)i + k] * (double)acc[3 * (size_t)i + k] * kFixInv;
+            }
+            // the gradient
+            AdjointArgs a{};
+            a.pos = e->pos;
+            a.atype = e->atype;
+            a.win = e->win;
+            a.atom_win = e->atom_win;
+            a.n_points = P;
+            a.point_win = e->point_win;
+            a.raw_e = e->raw_e;
+            a.raw_e0 = e->raw_e0;
+            a.q0 = e->pts.q0;
+            a.adj_off = e->adj_off;
+            a.adj_atoms = e->adj_atoms;
+            a.n_adj = (int)atoms.size();
+            a.cvec = e->cvec;
+            a.rmax = e->rmax;
+            a.vtot = e->vtot;
+            a.f_r0 = e->f_r0;
+            a.f_dr = e->f_dr;
+            a.f_inv = 1.0f / e->f_dr;
+            a.n_f = e->n_f;
+            a.ftab = e->ftab;
+            a.n_ftab = nF;
+            a.dJ_df = e->grads;
+            a.lam = e->lam;
+            a.g_table = e->g_raw;
+            a.n_g = e->n_g;
+            a.g_r0 = e->g_r0;
+            a.g_dr = e->g_dr;
+            a.g_inv = 1.0f / e->g_dr;
+            a.n_gtab = nG;
+            a.dJ_dg = e->grads + (size_t)W * nF;
+            a.n_mc = e->n_mc;
+            a.excl_start = e->excl_start;
+            a.excl = e->excl;
+            a.nbp = e->nbp;
+            a.n_lj_types = e->n_lj_types;
+            a.n_ljtab = ntt;
+            a.dJ_dA = e->grads + (size_t)W * (nF + nG);
+            a.dJ_dB = e->grads + (size_t)W * (nF + nG + ntt);
+            a.dihs = e->dihs;
+            a.dih_type = e->dih_type;
+            a.n_dihs = e->n_dihs;
+            a.sc14 = e->sc14;
+            launch_adjoint(a, e->stream);
+            ck(cudaGetLastError());
+        }
+        ck(cudaStreamSynchronize(e->stream));
+        std::vector<double> g((size_t)W * per_w);
+        ck(cudaMemcpy(g.data(), e->grads, sizeof(double) * g.size(), cudaMemcpyDeviceToHost));
+        const double inv = 1.0 / n_frames;
+        for (int w = 0; w < W; ++w) {
+            if (J) J[w] = Jw[w] * inv;
+            for (long long k = 0; k < nF; ++k)
+                if (dJ_df) dJ_df[w * nF + k] = g[(size_t)w * nF + k] * inv;
+            for (long long k = 0; k < nG; ++k)
+                if (dJ_dg) dJ_dg[w * nG + k] = g[(size_t)W * nF + (size_t)w * nG + k] * inv;
+            for (int k = 0; k < ntt; ++k) {
+                if (dJ_dA) dJ_dA[(size_t)w * ntt + k] = g[(size_t)W * (nF + nG) + (size_t)w * ntt + k] * inv;
+                if (dJ_dB) dJ_dB[(size_t)w * ntt + k] = g[(size_t)W * (nF + nG + ntt) + (size_t)w * ntt + k] * inv;
+            }
+        }
+        // restore the engine's state
+        ck(cudaMemcpy(e->pos, saved.data(), sizeof(float4) * N, cudaMemcpyHostToDevice));
+        ck(cudaMemcpy(e->d_step, &saved_step, sizeof saved_step, cudaMemcpyHostToDevice));
+        ck(cudaMemset(e->facc, 0, 3 * sizeof(unsigned long long) * N));
+    });
+    return rc;
 }
 
 int isspa_autotune(isspa_engine *e, int reps, int shape[7]) {

@@ -130,6 +130,46 @@ struct ListArgs {
     int *counts;
 };
 
+// ---- adjoint of the mean COM-axis force ------------------------------------
+struct AdjointArgs {
+    const float4 *pos;
+    const int2 *atype;
+    const WinDev *win;
+    const int *atom_win;
+    long long n_points;
+    const int *point_win;      // [Ptot]
+    const float4 *raw_e;       // field pass: E, w
+    const float4 *raw_e0;      // field pass: E0, n
+    const float4 *q0;          // point positions
+    const int *adj_off;        // [n_windows+1] ranges of adj_atoms per window
+    const int *adj_atoms;      // atoms with a nonzero weight
+    int n_adj;
+    const double *cvec;        // [Ntot][3] weights c_i
+    const float *rmax, *vtot;
+    float f_r0, f_dr, f_inv;
+    int n_f;
+    const float2 *ftab;
+    long long n_ftab;          // n_itypes * n_f
+    double *dJ_df;             // [n_windows][n_ftab]
+    double *lam;               // [Ptot] dJ/ds_p
+    const float *g_table;      // flat ISSPA_DENSITIES
+    int n_g;
+    float g_r0, g_dr, g_inv;
+    long long n_gtab;          // n_itypes * n_g
+    double *dJ_dg;             // [n_windows][n_gtab]
+    int n_mc;
+    const int *excl_start, *excl;
+    const int *nbp;            // [n_lj_types^2] packed LJ index
+    int n_lj_types;
+    int n_ljtab;               // n_lj_types (n_lj_types + 1) / 2
+    double *dJ_dA, *dJ_dB;     // [n_windows][n_ljtab]
+    const int4 *dihs;
+    const int *dih_type;
+    int n_dihs;
+    const float2 *sc14;
+};
+
+void launch_adjoint(const AdjointArgs &a, cudaStream_t s);
 void launch_field(const FieldArgs &a, int split, bool raw, cudaStream_t s);
 void launch_force(const ForceArgs &a, cudaStream_t s);
 void launch_nonbond(const NonbondArgs &a, cudaStream_t s);

@@ -124,6 +124,8 @@ SIGNATURES = [
     ("isspa_set_mc_points", C.c_int, [_P, _P, C.c_longlong]),
     ("isspa_clear_mc_points", C.c_int, [_P]),
     ("isspa_get_point_fields", C.c_int, [_P, _P, _P, _P, _P, _P, C.c_longlong]),
+    ("isspa_set_tables", C.c_int, [_P, _P, _P, _P, _P]),
+    ("isspa_adjoint_mean_force", C.c_int, [_P, C.c_int, _P, _P, _P, _P, _P, _P, _P]),
     ("isspa_neighbor_list", C.c_int, [_P, C.c_float, C.c_int, _P, _P]),
     ("isspa_cell_list", C.c_int, [_P, C.c_float, _P, _P]),
     ("isspa_measure_fp32_peak", C.c_int, [C.POINTER(C.c_double)]),

@@ -204,6 +204,32 @@ class Engine:
                   "point fields")
         return xyz, w, n, E, E0
 
+    # ------------------------------------------------ force field and gradient
+    def set_tables(self, g_table=None, e_table=None, f_table=None, lj_ab=None):
+        """Replace force-field tables (same shapes as the System's)."""
+        arrs = [None if t is None else np.ascontiguousarray(t, np.float32) for t in (g_table, e_table, f_table, lj_ab)]
+        abi.check(abi.lib().isspa_set_tables(self._h, *[None if a is None else _ptr(a) for a in arrs]), "set tables")
+
+    def adjoint_mean_force(self, steps, frames=None):
+        """Mean COM-axis force J per window and dJ/d(ISSPA_FORCES, ISSPA_DENSITIES,
+        LJ A, LJ B), averaged over frames (positions [F][Ntot][4] or None for the
+        current positions) whose MC points come from the Philox keys `steps`."""
+        w0 = self.windows[0]
+        W = self.n_windows
+        nt = len(w0.rmax)
+        nF, nG = nt * w0.f_table.shape[1], nt * w0.g_table.shape[1]
+        ntt = int(w0.n_lj_types) * (int(w0.n_lj_types) + 1) // 2
+        st = np.ascontiguousarray(steps, np.uint32)
+        fr = None if frames is None else np.ascontiguousarray(frames, np.float32).reshape(len(st), self.n_atoms, 4)
+        J = np.zeros(W)
+        df = np.zeros((W, nt, w0.f_table.shape[1]))
+        dg = np.zeros((W, nt, w0.g_table.shape[1]))
+        dA = np.zeros((W, ntt))
+        dB = np.zeros((W, ntt))
+        abi.check(abi.lib().isspa_adjoint_mean_force(self._h, len(st), None if fr is None else _ptr(fr), _ptr(st),
+                                                     _ptr(J), _ptr(df), _ptr(dg), _ptr(dA), _ptr(dB)), "adjoint")
+        return J, df, dg, dA, dB
+
     # --------------------------------------------------------------- lists
     def neighbor_list(self, rnn: float, max_per_atom: int = 576):
         n = self.windows[0].n_atoms

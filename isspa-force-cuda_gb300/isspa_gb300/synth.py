@@ -72,9 +72,52 @@ def forcefield(seed: int = 7, rmax: float = 12.0, n_mc: int = 50):
                gr2=np.stack([r_ex ** 2, r_end ** 2], 1).astype(np.float32).ravel(),
                lj_A=np.array([lj_ab[t * (t + 1) // 2 + t, 0] for t in range(nt)], np.float32),
                lj_B=np.array([lj_ab[t * (t + 1) // 2 + t, 1] for t in range(nt)], np.float32))
+    params = dict(sigma=sig, epsilon=eps, x0=x0, w=w, g0=g0, e_amp=amp, sigma_s=sig_s, epsilon_s=eps_s,
+                  r_cut=r_ex.copy())
     return dict(lj_ab=lj_ab, nbp=nbp, rmax=np.full(nt, rmax, np.float32),
                 g=g.astype(np.float32), e=e.astype(np.float32), f=f.astype(np.float32), omp=omp,
-                n_mc=n_mc)
+                n_mc=n_mc, params=params)
+
+
+def grid_r() -> np.ndarray:
+    """Radii of the tabulated grid (the fixtures' r = 0.05 + 0.1 k)."""
+    return GRID_R0 + GRID_DR * np.arange(GRID_N)
+
+
+def tables_from_params(p: dict, xp=np):
+    """Force-field tables as functions of the per-type parameters, in FP64.
+
+    sigma, epsilon (LJ, Lorentz-Berthelot) give the packed A/B coefficients and
+    the tabulated mean LJ force against one solvent site (zero below the fixed
+    radius r_cut, so that the table is smooth in every parameter); x0, w, g0
+    give the parabolic g(r): 0 below x0 - w, g0 - (g0/w^2)(r - x0)^2 up to where
+    it reaches 1, then 1.  `xp` may be numpy or torch (for automatic
+    differentiation in the tests)."""
+    sig, eps = p["sigma"], p["epsilon"]
+    nt = sig.shape[0]
+    r = xp.asarray(grid_r()) if xp is np else xp.tensor(grid_r(), dtype=sig.dtype)
+    A, B = [], []
+    for i in range(nt):
+        for j in range(i + 1):
+            s = 0.5 * (sig[i] + sig[j])
+            e = xp.sqrt(eps[i] * eps[j])
+            A.append(4 * e * s ** 12)
+            B.append(4 * e * s ** 6)
+    lj_ab = xp.stack([xp.stack(A), xp.stack(B)], 1)
+    g_rows, f_rows = [], []
+    for t in range(nt):
+        x0, w, g0 = p["x0"][t], p["w"][t], p["g0"][t]
+        alpha = g0 / w ** 2
+        r_ex = x0 - w
+        r_end = x0 + xp.sqrt((g0 - 1.0) / alpha)
+        par = g0 - alpha * (r - x0) ** 2
+        g_rows.append(xp.where(r < r_ex, xp.zeros_like(r), xp.where(r <= r_end, par, xp.ones_like(r))))
+        s = 0.5 * (sig[t] + p["sigma_s"])
+        e = xp.sqrt(eps[t] * p["epsilon_s"])
+        sr = s / r
+        lj = 24 * e / r * (2 * sr ** 12 - sr ** 6)
+        f_rows.append(xp.where(r >= float(p["r_cut"][t]), lj, xp.zeros_like(r)))
+    return dict(lj_ab=lj_ab, g=xp.stack(g_rows), f=xp.stack(f_rows))
 
 
 def _grow_chain(rng, length: int, start: np.ndarray, max_tries: int = 200) -> Optional[np.ndarray]:

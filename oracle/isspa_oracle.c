@@ -432,7 +432,7 @@ void orc_angles(int na, const int *atoms, const float *params, const float *pos,
 /* K7: dihedral + scaled 1-4, src/dih_force_cuda.cu:48-135. */
 void orc_dihedrals(int nd, const int *atoms, const int *types, const float *params,
                    const float *scaled14, const int *lj_type, const int *nb_parm_index,
-                   int n_types, const float *lj_ab, const float *pos, float box,
+                   int n_types, const double *lj_ab, const float *pos, float box,
                    int with_14, double *f) {
     const float L = box, h = 0.5f * box;
     for (int d = 0; d < nd; ++d) {
@@ -591,4 +591,187 @@ void orc_cell_index(int n, const float *pos, float rc, const int ncell[3], int *
         int cx = (int)(pos[4 * i] / rc), cy = (int)(pos[4 * i + 1] / rc), cz = (int)(pos[4 * i + 2] / rc);
         cell[i] = cx * ncell[1] * ncell[2] + cy * ncell[2] + cz;
     }
+}
+
+/* ---------------------------------------------------------------------------
+ * Adjoint of J = sum_i c_i . F_i for one frame, in FP64 (naive reference
+ * gradient).  Writing the IS-SPA force of point p on atom i as
+ *   F_ip = s_p G_ip + H_ip,   s_p = w_p / n_p,
+ * with G the multipole and tabulated-LJ parts per unit density and H the
+ * constant-density-dielectric part (isspa_force_cuda.cu:274-312), the
+ * derivatives are
+ *   dJ/ds_p        = sum_i c_i . G_ip                       (lambda_p)
+ *   dJ/dT_f[k]     = sum_{i,p} c_i . (-vtot_i s_p r/d) * lerp weight of k
+ *   dJ/dT_g[k]     = sum_p lambda_p / n_p * dw_p/dT_g[k],  w_p = prod_j g_j
+ * and, for the nonbond LJ (nonbond_force_cuda.cu:131-132) and the scaled 1-4
+ * LJ (dih_force_cuda.cu:70-74), the coefficients enter linearly.
+ * ------------------------------------------------------------------------- */
+double orc_adjoint(const orc_isspa_sys *s, const orc_nb_sys *nb, int n_mc, const float *pts,
+                   const double *c, int nd, const int *dih_atoms, const int *dih_types,
+                   const float *scaled14, double *dJ_df, double *dJ_dg, double *dJ_dA,
+                   double *dJ_dB) {
+    const int N = s->n_atoms;
+    const long P = (long)N * n_mc;
+    const float L = s->box, h = 0.5f * s->box;
+    const double p0 = ORC_P0, q0 = ORC_Q0, o0 = ORC_O0;
+    double *w = (double *)malloc(sizeof(double) * (size_t)P);
+    int *cnt = (int *)malloc(sizeof(int) * (size_t)P);
+    double *E = (double *)malloc(sizeof(double) * 3 * (size_t)P);
+    double *E0 = (double *)malloc(sizeof(double) * 3 * (size_t)P);
+    double *lam = (double *)calloc((size_t)P, sizeof(double));
+    orc_field(s, n_mc, pts, w, cnt, E, E0);
+    const float f_inv = 1.0f / s->f_dr, g_inv = 1.0f / s->g_dr;
+    const long nF = (long)s->n_itypes * s->n_f, nG = (long)s->n_itypes * s->n_g;
+    double J = 0.0;
+    /* IS-SPA force part: value, lambda_p, force-table adjoint */
+    for (long p = 0; p < P; ++p) {
+        const double *Ep = E + 3 * p;
+        const double mag = sqrt(Ep[0] * Ep[0] + Ep[1] * Ep[1] + Ep[2] * Ep[2]);
+        double lg[3];
+        orc_langevin(mag, lg);
+        const double eh[3] = {mag > 0 ? Ep[0] / mag : 0, mag > 0 ? Ep[1] / mag : 0, mag > 0 ? Ep[2] / mag : 0};
+        const double inv_n = 1.0 / cnt[p], sp = w[p] * inv_n;
+        const double e03[3] = {E0[3 * p] / 3.0, E0[3 * p + 1] / 3.0, E0[3 * p + 2] / 3.0};
+        for (int i = 0; i < N; ++i) {
+            const double *ci = c + 3 * i;
+            if (ci[0] == 0.0 && ci[1] == 0.0 && ci[2] == 0.0) continue;
+            const float *xi = s->pos + 4 * i;
+            const int it = s->isspa_type[i];
+            const float rm = s->rmax[it];
+            const double vt = s->vtot[it], qi = xi[3];
+            const float rx = mimg(pts[3 * p] - xi[0], L, h), ry = mimg(pts[3 * p + 1] - xi[1], L, h),
+                        rz = mimg(pts[3 * p + 2] - xi[2], L, h);
+            const float d2 = dist2f(rx, ry, rz);
+            const double r[3] = {rx, ry, rz};
+            const double dd2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2], dd = sqrt(dd2);
+            const double Rz = (eh[0] * r[0] + eh[1] * r[1] + eh[2] * r[2]) / dd;
+            const double dp1 = 3.0 * Rz, dp2 = 7.5 * Rz * Rz - 1.5, dp3 = (17.5 * Rz * Rz - 7.5) * Rz;
+            const double t1 = p0 * lg[0] / (dd2 * dd), t2 = q0 * lg[1] / (dd2 * dd2), t3 = o0 * lg[2] / (dd2 * dd2 * dd);
+            double G[3], H[3] = {0, 0, 0};
+            for (int k = 0; k < 3; ++k) {
+                const double mu = t1 * (r[k] * dp1 / dd - eh[k]) + t2 * (r[k] * dp2 / dd - dp1 * eh[k]) +
+                                  t3 * (r[k] * dp3 / dd - dp2 * eh[k]);
+                G[k] = -qi * vt * mu;
+            }
+            if (d2 <= rm * rm) {
+                const float dist = sqrtf(d2);
+                const int bin = (int)fmaf(dist - s->f_r0, f_inv, 0.5f);
+                if (bin >= 0 && bin < s->n_f) {
+                    const double fr = (dd - ((double)s->f_r0 + bin * (double)s->f_dr)) / s->f_dr;
+                    const long fi = (long)it * s->n_f + bin;
+                    const double tab = s->f_table[fi] * (1.0 - fr) + s->f_table[fi + 1] * fr;
+                    double cr = 0.0;
+                    for (int k = 0; k < 3; ++k) {
+                        G[k] += -vt * tab * r[k] / dd;
+                        cr += ci[k] * (-vt * sp * r[k] / dd);
+                    }
+                    dJ_df[fi] += cr * (1.0 - fr);
+                    if (fi + 1 < nF) dJ_df[fi + 1] += cr * fr;
+                }
+            } else {
+                const double fs = -qi * p0 / (dd2 * dd);
+                const double pdr = 3.0 * (e03[0] * r[0] + e03[1] * r[1] + e03[2] * r[2]) / dd2;
+                for (int k = 0; k < 3; ++k) H[k] = fs * (pdr * r[k] - e03[k]) * vt * inv_n;
+            }
+            for (int k = 0; k < 3; ++k) {
+                J += ci[k] * (sp * G[k] + H[k]);
+                lam[p] += ci[k] * G[k];
+            }
+        }
+    }
+    /* density-table adjoint through w_p = prod_j g_j (isspa_force_cuda.cu:157-167) */
+    for (long p = 0; p < P; ++p) {
+        if (lam[p] == 0.0) continue;
+        const int a = (int)(p / n_mc);
+        const float rm = s->rmax[s->isspa_type[a]];
+        const double dJdw = lam[p] / cnt[p];
+        int zeros = 0, forced_zero = 0;
+        double prod_nz = 1.0;
+        for (int pass = 0; pass < 2; ++pass) {
+            for (int j = 0; j < N; ++j) {
+                const float *xj = s->pos + 4 * j;
+                const float rx = mimg(pts[3 * p] - xj[0], L, h), ry = mimg(pts[3 * p + 1] - xj[1], L, h),
+                            rz = mimg(pts[3 * p + 2] - xj[2], L, h);
+                const float d2 = dist2f(rx, ry, rz);
+                if (!(d2 <= rm * rm)) continue;
+                const float dist = sqrtf(d2);
+                const int bin = (int)((dist - s->g_r0) * g_inv);
+                if (bin < 0) {
+                    forced_zero = 1;
+                    continue;
+                }
+                if (bin >= s->n_g - 1) continue;
+                const double dd = sqrt((double)rx * rx + (double)ry * ry + (double)rz * rz);
+                const double fr = (dd - ((double)s->g_r0 + bin * (double)s->g_dr)) / s->g_dr;
+                const long gi = (long)s->isspa_type[j] * s->n_g + bin;
+                const double g = s->g_table[gi] * (1.0 - fr) + s->g_table[gi + 1] * fr;
+                if (pass == 0) {
+                    if (g == 0.0) ++zeros;
+                    else prod_nz *= g;
+                } else {
+                    double others;
+                    if (forced_zero || zeros >= 2) others = 0.0;
+                    else if (zeros == 1) others = g == 0.0 ? prod_nz : 0.0;
+                    else others = prod_nz / g;
+                    const double d = dJdw * others;
+                    dJ_dg[gi] += d * (1.0 - fr);
+                    if (gi + 1 < nG) dJ_dg[gi + 1] += d * fr;
+                }
+            }
+        }
+    }
+    /* nonbond: value and LJ coefficient adjoint (nonbond_force_cuda.cu:123-162) */
+    {
+        const double epf = 1.0 - 1.0 / (double)ORC_EP;
+        for (int i = 0; i < N; ++i) {
+            const double *ci = c + 3 * i;
+            if (ci[0] == 0.0 && ci[1] == 0.0 && ci[2] == 0.0) continue;
+            const float *xi = nb->pos + 4 * i;
+            for (int j = 0; j < N; ++j) {
+                if (j == i) continue;
+                const float *xj = nb->pos + 4 * j;
+                const float rx = mimg(xi[0] - xj[0], L, h), ry = mimg(xi[1] - xj[1], L, h), rz = mimg(xi[2] - xj[2], L, h);
+                const float d2 = dist2f(rx, ry, rz);
+                const double r[3] = {rx, ry, rz};
+                const double dd2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2], dd = sqrt(dd2);
+                const double qq = (double)xi[3] * xj[3];
+                const float rmj = nb->rmax[nb->isspa_type[j]];
+                const float two = 2.0f * rmj;
+                double fs = d2 > two * two ? -2.0 * qq * epf / (3.0 * dd2 * dd)
+                                           : -qq * epf * (8.0 * rmj - 3.0 * dd) / (24.0 * (double)rmj * rmj * rmj * rmj);
+                const double cr = ci[0] * r[0] + ci[1] * r[1] + ci[2] * r[2];
+                if (!orc_excluded(nb, i, j)) {
+                    const int k = nb->nb_parm_index[nb->n_types * nb->lj_type[i] + nb->lj_type[j]];
+                    const double r6 = 1.0 / (dd2 * dd2 * dd2);
+                    fs += r6 * (12.0 * nb->lj_ab[2 * k] * r6 - 6.0 * nb->lj_ab[2 * k + 1]) / dd2 + qq / (dd2 * dd);
+                    dJ_dA[k] += cr * 12.0 * r6 * r6 / dd2;
+                    dJ_dB[k] += cr * (-6.0) * r6 / dd2;
+                }
+                J += cr * fs;
+            }
+        }
+    }
+    /* scaled 1-4 terms of the dihedrals (dih_force_cuda.cu:60-82) */
+    for (int d = 0; d < nd; ++d) {
+        const int ax = dih_atoms[4 * d], az = dih_atoms[4 * d + 2], aw = dih_atoms[4 * d + 3];
+        if (!(az > 0 && aw > 0)) continue;
+        const double *cx = c + 3 * ax, *cw = c + 3 * aw;
+        const double dc[3] = {cx[0] - cw[0], cx[1] - cw[1], cx[2] - cw[2]};
+        if (dc[0] == 0.0 && dc[1] == 0.0 && dc[2] == 0.0) continue;
+        const int t = dih_types[d];
+        const int k = nb->nb_parm_index[nb->n_types * nb->lj_type[ax] + nb->lj_type[aw]];
+        double r14[3];
+        rvec(nb->pos, ax, aw, L, h, r14);
+        const double rm = r14[0] * r14[0] + r14[1] * r14[1] + r14[2] * r14[2];
+        const double r6 = 1.0 / (rm * rm * rm);
+        const double scee = scaled14[2 * t], scnb = scaled14[2 * t + 1];
+        const double fe = (double)nb->pos[4 * ax + 3] * nb->pos[4 * aw + 3] / (rm * sqrt(rm) * scee);
+        const double fv = r6 * (12.0 * nb->lj_ab[2 * k] * r6 - 6.0 * nb->lj_ab[2 * k + 1]) / (scnb * rm);
+        const double cr = dc[0] * r14[0] + dc[1] * r14[1] + dc[2] * r14[2];
+        J += cr * (fe + fv);
+        dJ_dA[k] += cr * 12.0 * r6 * r6 / (scnb * rm);
+        dJ_dB[k] += cr * (-6.0) * r6 / (scnb * rm);
+    }
+    free(w); free(cnt); free(E); free(E0); free(lam);
+    return J;
 }

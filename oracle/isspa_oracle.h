@@ -38,9 +38,9 @@ typedef struct {
     const float *rmax;       /* [n_itypes] */
     const float *vtot;       /* [n_itypes], isspa_class.cpp:41 */
     int n_g, n_e, n_f;       /* rows per type of the three tables */
-    const float *g_table;    /* [n_itypes*n_g] (+ zero padding, see below) */
-    const float *e_table;    /* [n_itypes*n_e] */
-    const float *f_table;    /* [n_itypes*n_f] */
+    const double *g_table;   /* [n_itypes*n_g] (+ zero padding); values in FP64 */
+    const double *e_table;   /* [n_itypes*n_e] */
+    const double *f_table;   /* [n_itypes*n_f] */
     float g_r0, g_dr, e_r0, e_dr, f_r0, f_dr;
     float box;
 } orc_isspa_sys;
@@ -52,7 +52,7 @@ typedef struct {
     int n_types;
     const int *lj_type;        /* [n_atoms] 0-based */
     const int *nb_parm_index;  /* [n_types*n_types] 0-based index into lj_ab */
-    const float *lj_ab;        /* [n_types*(n_types+1)/2][2] A, B */
+    const double *lj_ab;       /* [n_types*(n_types+1)/2][2] A, B */
     const int *n_excl_cum;     /* [n_atoms] cumulative counts */
     const int *excl_list;      /* [excl_len] 0-based */
     const int *isspa_type;     /* [n_atoms] */
@@ -98,7 +98,7 @@ void orc_bonds(int nb, const int *atoms, const float *params, const float *pos, 
 void orc_angles(int na, const int *atoms, const float *params, const float *pos, float box, double *f);
 void orc_dihedrals(int nd, const int *atoms, const int *types, const float *params,
                    const float *scaled14, const int *lj_type, const int *nb_parm_index,
-                   int n_types, const float *lj_ab, const float *pos, float box,
+                   int n_types, const double *lj_ab, const float *pos, float box,
                    int with_14, double *f);
 
 /* Umbrella COM restraint (us_force_cuda.cu:14-48); com_out[2][3]. */
@@ -121,6 +121,19 @@ long orc_neighbor_list(const orc_nb_sys *s, float rnn2, int max_per_atom, int *r
 void orc_cell_index(int n, const float *pos, float rc, const int ncell[3], int *cell);
 
 void orc_set_threads(int n);
+
+/* Adjoint of J = sum_i c_i . F_i for one frame (naive FP64 reference gradient).
+ * c: [N][3] weights (zero for atoms outside the restraint groups).  F_i is the
+ * IS-SPA force on the given points plus the nonbond force plus the scaled 1-4
+ * term of the dihedrals.  Accumulates into
+ *   dJ_df [n_itypes*n_f]  (ISSPA_FORCES entries),
+ *   dJ_dg [n_itypes*n_g]  (ISSPA_DENSITIES entries),
+ *   dJ_dA, dJ_dB [n_types*(n_types+1)/2]  (packed LJ coefficients),
+ * and returns J. */
+double orc_adjoint(const orc_isspa_sys *s, const orc_nb_sys *nb, int n_mc, const float *pts,
+                   const double *c, int nd, const int *dih_atoms, const int *dih_types,
+                   const float *scaled14, double *dJ_df, double *dJ_dg, double *dJ_dA,
+                   double *dJ_dB);
 
 #ifdef __cplusplus
 }

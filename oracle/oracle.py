@@ -69,35 +69,46 @@ def _i32(a):
     return np.ascontiguousarray(a, dtype=np.int32)
 
 
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
 def _pad(t, extra):
-    t = _f32(t).ravel()
-    return np.concatenate([t, np.zeros(extra, np.float32)])
+    t = _f64(t).ravel()
+    return np.concatenate([t, np.zeros(extra, np.float64)])
 
 
 class Oracle:
-    """Oracle bound to one system (a ``isspa_gb300.System``-like object)."""
+    """Oracle bound to one system (a ``isspa_gb300.System``-like object).
 
-    def __init__(self, system, threads: int = 0):
+    Table values (ISSPA_DENSITIES / _EFIELD / _FORCES, LJ A and B) are held in
+    FP64; `tables` may supply FP64 values that override the system's float ones
+    (finite differences in the force-field parameters)."""
+
+    def __init__(self, system, threads: int = 0, tables=None):
         s = system
         self.s = s
         self.n = int(s.n_atoms)
         self.n_mc = int(s.n_mc)
         self._keep = []
         k = self._keep
+        tables = tables or {}
         pos = _f32(s.pos).reshape(-1, 4)
         k.append(pos)
         self.pos = pos
         ityp = _i32(s.isspa_type); k.append(ityp)
         rmax = _f32(s.rmax); k.append(rmax)
         vtot = _f32(s.vtot()); k.append(vtot)
-        pad = max(s.g_table.shape[1], s.e_table.shape[1], s.f_table.shape[1]) + 1
-        g = _pad(s.g_table, pad); e = _pad(s.e_table, pad); f = _pad(s.f_table, pad)
+        gt = tables.get("g", s.g_table); et = tables.get("e", s.e_table); ft = tables.get("f", s.f_table)
+        pad = max(gt.shape[1], et.shape[1], ft.shape[1]) + 1
+        g = _pad(gt, pad); e = _pad(et, pad); f = _pad(ft, pad)
         k.extend([g, e, f])
         self.isys = _IsspaSys(self.n, _p(pos), _p(ityp), int(len(rmax)), _p(rmax), _p(vtot),
-                              s.g_table.shape[1], s.e_table.shape[1], s.f_table.shape[1],
+                              gt.shape[1], et.shape[1], ft.shape[1],
                               _p(g), _p(e), _p(f), s.g_r0, s.g_dr, s.e_r0, s.e_dr,
                               s.f_r0, s.f_dr, s.box)
-        ljt = _i32(s.lj_type); nbp = _i32(s.nb_parm_index); lj = _f32(s.lj_ab)
+        ljt = _i32(s.lj_type); nbp = _i32(s.nb_parm_index); lj = _f64(tables.get("lj_ab", s.lj_ab))
+        self.lj = lj
         exc = _i32(s.n_excl_cum); exl = _i32(s.excl_list if len(s.excl_list) else [-1])
         k.extend([ljt, nbp, lj, exc, exl])
         self.nsys = _NbSys(self.n, _p(pos), int(s.n_lj_types), _p(ljt), _p(nbp), _p(lj),
@@ -145,7 +156,7 @@ class Oracle:
         aa = _i32(s.angle_atoms); ap = _f32(s.angle_params)
         da = _i32(s.dih_atoms); dt = _i32(s.dih_types); dp = _f32(s.dih_params)
         sc = _f32(s.scaled14)
-        ljt = _i32(s.lj_type); nbp = _i32(s.nb_parm_index); lj = _f32(s.lj_ab)
+        ljt = _i32(s.lj_type); nbp = _i32(s.nb_parm_index); lj = self.lj
         if len(ba):
             L.orc_bonds(len(ba), _p(ba), _p(bp), _p(self.pos), C.c_float(s.box), _p(f))
         if len(aa):
@@ -190,6 +201,65 @@ class Oracle:
         cell = np.zeros(self.n, np.int32)
         lib().orc_cell_index(self.n, _p(self.pos), C.c_float(rc), _p(nc), _p(cell))
         return cell
+
+    def com_axis_weights(self):
+        """Per-atom weights c_i of the mean COM-axis force J = sum_i c_i . F_i:
+        +n/2 on restraint group 0, -n/2 on group 1, n the unit vector from the
+        group-1 to the group-0 centre of mass (mass fractions, minimum image as
+        us_force_cuda.cu:30-31)."""
+        s = self.s
+        c = np.zeros((self.n, 3))
+        if not s.us_on:
+            return c
+        _, com = self.us()
+        d = com[0] - com[1]
+        d -= s.box * np.where(d > 0.5 * s.box, 1.0, np.where(d < -0.5 * s.box, -1.0, 0.0))
+        nh = d / np.linalg.norm(d)
+        for a, g in np.asarray(s.bias_list).reshape(-1, 2):
+            c[a] += (0.5 if g == 0 else -0.5) * nh
+        return c
+
+    def adjoint(self, pts, c=None):
+        """FP64 adjoint of J = sum_i c_i . F_i (IS-SPA + nonbond + 1-4) for one
+        frame: returns J and dJ/d(ISSPA_FORCES, ISSPA_DENSITIES, LJ A, LJ B)."""
+        s = self.s
+        c = self.com_axis_weights() if c is None else np.ascontiguousarray(c, np.float64)
+        pts = _f32(pts).reshape(-1, 3)
+        nt = len(s.rmax)
+        df = np.zeros(nt * s.f_table.shape[1])
+        dg = np.zeros(nt * s.g_table.shape[1])
+        ntt = int(s.n_lj_types) * (int(s.n_lj_types) + 1) // 2
+        dA = np.zeros(ntt)
+        dB = np.zeros(ntt)
+        da = _i32(s.dih_atoms if len(s.dih_atoms) else np.zeros((1, 4)))
+        dt = _i32(s.dih_types if len(s.dih_types) else np.zeros(1))
+        sc = _f32(s.scaled14 if len(s.scaled14) else np.ones((1, 2)))
+        cc = np.ascontiguousarray(c, np.float64)
+        L = lib()
+        L.orc_adjoint.restype = C.c_double
+        J = L.orc_adjoint(C.byref(self.isys), C.byref(self.nsys), self.n_mc, _p(pts), _p(cc),
+                          int(len(s.dih_atoms)), _p(da), _p(dt), _p(sc), _p(df), _p(dg), _p(dA), _p(dB))
+        return J, df.reshape(nt, -1), dg.reshape(nt, -1), dA, dB
+
+    def mean_force(self, pts, c=None):
+        """J = sum_i c_i . F_i over every non-restraint force term of one frame."""
+        c = self.com_axis_weights() if c is None else c
+        J = self.adjoint(pts, c)[0]
+        s = self.s
+        f = np.zeros((self.n, 3))
+        L = lib()
+        ba = _i32(s.bond_atoms); bp = _f32(s.bond_params)
+        aa = _i32(s.angle_atoms); ap = _f32(s.angle_params)
+        if len(ba):
+            L.orc_bonds(len(ba), _p(ba), _p(bp), _p(self.pos), C.c_float(s.box), _p(f))
+        if len(aa):
+            L.orc_angles(len(aa), _p(aa), _p(ap), _p(self.pos), C.c_float(s.box), _p(f))
+        if len(s.dih_atoms):
+            L.orc_dihedrals(len(s.dih_atoms), _p(_i32(s.dih_atoms)), _p(_i32(s.dih_types)),
+                            _p(_f32(s.dih_params)), _p(_f32(s.scaled14)), _p(_i32(s.lj_type)),
+                            _p(_i32(s.nb_parm_index)), int(s.n_lj_types), _p(self.lj), _p(self.pos),
+                            C.c_float(s.box), 0, _p(f))
+        return J + float(np.sum(np.asarray(c) * f))
 
     def total_force(self, seed: int, step: int, window: int = 0, pts=None):
         """Forces of one full step, in the reference's call order
