@@ -115,15 +115,29 @@ void orc_mc_points(const orc_isspa_sys *s, int n_mc, uint64_t seed, uint32_t ste
  * Flattened table rows: bin+1 may run into the next type's row as in the
  * reference; the caller pads each table with zeros at its end.
  * ------------------------------------------------------------------------- */
+static void field_impl(const orc_isspa_sys *s, int n_mc, const float *pts, const long *idx, long count,
+                       double *w, int *cnt, double *efield, double *e0field);
+
 void orc_field(const orc_isspa_sys *s, int n_mc, const float *pts, double *w, int *cnt,
                double *efield, double *e0field) {
+    field_impl(s, n_mc, pts, NULL, (long)s->n_atoms * n_mc, w, cnt, efield, e0field);
+}
+
+void orc_field_at(const orc_isspa_sys *s, int n_mc, const float *pts, const long *idx, long count,
+                  double *w, int *cnt, double *efield, double *e0field) {
+    field_impl(s, n_mc, pts, idx, count, w, cnt, efield, e0field);
+}
+
+/* Outputs at position q for point idx[q] (or q when idx is NULL). */
+static void field_impl(const orc_isspa_sys *s, int n_mc, const float *pts, const long *idx, long count,
+                       double *w, int *cnt, double *efield, double *e0field) {
     const int N = s->n_atoms;
-    const long P = (long)N * n_mc;
     const float L = s->box, h = 0.5f * s->box;
     const double e0 = orc_e0();
     const float g_inv = 1.0f / s->g_dr;
 #pragma omp parallel for schedule(dynamic, 64)
-    for (long p = 0; p < P; ++p) {
+    for (long q = 0; q < count; ++q) {
+        const long p = idx ? idx[q] : q;
         const int a = (int)(p / n_mc);
         const float rm = s->rmax[s->isspa_type[a]];
         const float rm2 = rm * rm;
@@ -160,11 +174,11 @@ void orc_field(const orc_isspa_sys *s, int n_mc, const float *pts, double *w, in
                 E0[0] -= c * dx; E0[1] -= c * dy; E0[2] -= c * dz;
             }
         }
-        w[p] = wp;
-        cnt[p] = n;
+        w[q] = wp;
+        cnt[q] = n;
         for (int k = 0; k < 3; ++k) {
-            efield[3 * p + k] = E[k];
-            e0field[3 * p + k] = E0[k];
+            efield[3 * q + k] = E[k];
+            e0field[3 * q + k] = E0[k];
         }
     }
 }
@@ -224,9 +238,26 @@ void orc_langevin(double x, double out[3]) {
  * A zero field (|E| == 0) contributes no multipole force (the reference
  * divides 0/0 there).
  * ------------------------------------------------------------------------- */
+static void force_impl(const orc_isspa_sys *s, int n_mc, const float *pts, const double *w, const int *cnt,
+                       const double *efield, const double *e0field, int term_mask, const int *atoms,
+                       int n_sel, double *f);
+
 void orc_isspa_force(const orc_isspa_sys *s, int n_mc, const float *pts, const double *w,
                      const int *cnt, const double *efield, const double *e0field,
                      int term_mask, double *f) {
+    force_impl(s, n_mc, pts, w, cnt, efield, e0field, term_mask, NULL, s->n_atoms, f);
+}
+
+void orc_isspa_force_atoms(const orc_isspa_sys *s, int n_mc, const float *pts, const double *w,
+                           const int *cnt, const double *efield, const double *e0field, int term_mask,
+                           const int *atoms, int n_sel, double *f) {
+    force_impl(s, n_mc, pts, w, cnt, efield, e0field, term_mask, atoms, n_sel, f);
+}
+
+/* Force on atoms[ii] (or ii when atoms is NULL) accumulated into f[ii]. */
+static void force_impl(const orc_isspa_sys *s, int n_mc, const float *pts, const double *w, const int *cnt,
+                       const double *efield, const double *e0field, int term_mask, const int *atoms,
+                       int n_sel, double *f) {
     const int N = s->n_atoms;
     const long P = (long)N * n_mc;
     const float L = s->box, h = 0.5f * s->box;
@@ -253,7 +284,8 @@ void orc_isspa_force(const orc_isspa_sys *s, int n_mc, const float *pts, const d
         q[8] = e0field[3 * p] / 3.0; q[9] = e0field[3 * p + 1] / 3.0; q[10] = e0field[3 * p + 2] / 3.0;
     }
 #pragma omp parallel for schedule(dynamic, 1)
-    for (int i = 0; i < N; ++i) {
+    for (int ii = 0; ii < n_sel; ++ii) {
+        const int i = atoms ? atoms[ii] : ii;
         const float *xi = s->pos + 4 * i;
         const int it = s->isspa_type[i];
         const float rm = s->rmax[it];
@@ -311,7 +343,7 @@ void orc_isspa_force(const orc_isspa_sys *s, int n_mc, const float *pts, const d
                 F[2] += fs * (pdr * dz - q[10]) * igo;
             }
         }
-        f[3 * i] += F[0]; f[3 * i + 1] += F[1]; f[3 * i + 2] += F[2];
+        f[3 * ii] += F[0]; f[3 * ii + 1] += F[1]; f[3 * ii + 2] += F[2];
     }
     free(pp);
 }
@@ -338,12 +370,22 @@ static int orc_excluded(const orc_nb_sys *s, int i, int j) {
  * 2 rmax[type j] => -2q1q2(1-1/ep)/(3r^3), else -q1q2(1-1/ep)(8rmax-3r)/(24
  * rmax^4).  Force on atom i only.
  * ------------------------------------------------------------------------- */
-void orc_nonbond(const orc_nb_sys *s, int term_mask, double *f) {
+static void nonbond_impl(const orc_nb_sys *s, int term_mask, const int *atoms, int n_sel, double *f);
+
+void orc_nonbond(const orc_nb_sys *s, int term_mask, double *f) { nonbond_impl(s, term_mask, NULL, s->n_atoms, f); }
+
+void orc_nonbond_atoms(const orc_nb_sys *s, int term_mask, const int *atoms, int n_sel, double *f) {
+    nonbond_impl(s, term_mask, atoms, n_sel, f);
+}
+
+/* Force on atoms[ii] (or ii when atoms is NULL) accumulated into f[ii]. */
+static void nonbond_impl(const orc_nb_sys *s, int term_mask, const int *atoms, int n_sel, double *f) {
     const int N = s->n_atoms;
     const float L = s->box, h = 0.5f * s->box;
     const double epf = 1.0 - 1.0 / (double)ORC_EP;
 #pragma omp parallel for schedule(dynamic, 4)
-    for (int i = 0; i < N; ++i) {
+    for (int ii = 0; ii < n_sel; ++ii) {
+        const int i = atoms ? atoms[ii] : ii;
         const float *xi = s->pos + 4 * i;
         double F[3] = {0, 0, 0};
         for (int j = 0; j < N; ++j) {
@@ -379,7 +421,7 @@ void orc_nonbond(const orc_nb_sys *s, int term_mask, double *f) {
             }
             F[0] += fs * dx; F[1] += fs * dy; F[2] += fs * dz;
         }
-        f[3 * i] += F[0]; f[3 * i + 1] += F[1]; f[3 * i + 2] += F[2];
+        f[3 * ii] += F[0]; f[3 * ii + 1] += F[1]; f[3 * ii + 2] += F[2];
     }
 }
 

@@ -85,6 +85,16 @@ void orc_isspa_force(const orc_isspa_sys *s, int n_mc, const float *pts, const d
                      const int *cnt, const double *efield, const double *e0field,
                      int term_mask, double *f /* [N][3], accumulated into */);
 
+/* Subsets for large systems: fields at the listed point indices (outputs at
+ * list positions), IS-SPA and nonbond forces on the listed atoms (f[k] for
+ * atoms[k]), from all points / all partners. */
+void orc_field_at(const orc_isspa_sys *s, int n_mc, const float *pts, const long *idx, long count,
+                  double *w, int *cnt, double *efield, double *e0field);
+void orc_isspa_force_atoms(const orc_isspa_sys *s, int n_mc, const float *pts, const double *w,
+                           const int *cnt, const double *efield, const double *e0field, int term_mask,
+                           const int *atoms, int n_sel, double *f);
+void orc_nonbond_atoms(const orc_nb_sys *s, int term_mask, const int *atoms, int n_sel, double *f);
+
 /* Langevin polarisation averages <P1>, <P2>, <P3> for field magnitude x. */
 void orc_langevin(double x, double out[3]);
 /* 1: evaluate them with the reference's float closed forms (diagnostic). */

@@ -142,6 +142,34 @@ class Oracle:
                               _p(np.ascontiguousarray(E0)), int(terms), _p(f))
         return f
 
+    # -- subsets (large systems) -------------------------------------------
+    def field_at(self, pts, idx):
+        """Field pass at the point indices `idx` only (pts: all points)."""
+        pts = _f32(pts).reshape(-1, 3)
+        idx = np.ascontiguousarray(idx, np.int64)
+        n = len(idx)
+        w = np.zeros(n); cnt = np.zeros(n, np.int32); E = np.zeros((n, 3)); E0 = np.zeros((n, 3))
+        lib().orc_field_at(C.byref(self.isys), self.n_mc, _p(pts), _p(idx), C.c_long(n), _p(w), _p(cnt),
+                           _p(E), _p(E0))
+        return w, cnt, E, E0
+
+    def isspa_force_atoms(self, pts, field, atoms, terms: int = 7):
+        """IS-SPA force on `atoms` from all points, given the field of all points."""
+        pts = _f32(pts).reshape(-1, 3)
+        w, cnt, E, E0 = field
+        at = _i32(atoms)
+        f = np.zeros((len(at), 3))
+        lib().orc_isspa_force_atoms(C.byref(self.isys), self.n_mc, _p(pts), _p(np.ascontiguousarray(w, np.float64)),
+                                    _p(_i32(cnt)), _p(np.ascontiguousarray(E, np.float64)),
+                                    _p(np.ascontiguousarray(E0, np.float64)), int(terms), _p(at), len(at), _p(f))
+        return f
+
+    def nonbond_atoms(self, atoms, terms: int = 7):
+        at = _i32(atoms)
+        f = np.zeros((len(at), 3))
+        lib().orc_nonbond_atoms(C.byref(self.nsys), int(terms), _p(at), len(at), _p(f))
+        return f
+
     # -- pair / bonded terms ---------------------------------------------------
     def nonbond(self, terms: int = 7) -> np.ndarray:
         f = np.zeros((self.n, 3))
