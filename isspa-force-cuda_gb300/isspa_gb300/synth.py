@@ -158,26 +158,39 @@ def _grow_chain(rng, length: int, start: np.ndarray, max_tries: int = 200) -> Op
 
 
 def make_chains(n_chains: int, length: int, box: float, rng) -> np.ndarray:
-    """Self-avoiding chains placed without overlap (min image distance >= 3 A)."""
-    placed = np.zeros((0, 3))
+    """Self-avoiding chains placed without overlap (min image distance >= 3 A),
+    checked against already placed atoms through a 3 A cell grid."""
+    m = max(1, int(box // 3.0))
+    cell = box / m
+    grid = {}
     out = []
+
+    def clash(xw):
+        for p in xw:
+            c = np.floor(p / cell).astype(int) % m
+            for dx in (-1, 0, 1):
+                for dy in (-1, 0, 1):
+                    for dz in (-1, 0, 1):
+                        lst = grid.get(((c[0] + dx) % m, (c[1] + dy) % m, (c[2] + dz) % m))
+                        if not lst:
+                            continue
+                        d = np.asarray(lst) - p
+                        d -= box * np.round(d / box)
+                        if np.min(np.einsum("ij,ij->i", d, d)) < 9.0:
+                            return True
+        return False
+
     for c in range(n_chains):
-        for _ in range(500):
+        for _ in range(2000):
             x = _grow_chain(rng, length, rng.uniform(0, box, 3))
             if x is None:
                 continue
             xw = np.mod(x, box)
-            if len(placed):
-                ok = True
-                for k in range(0, length):
-                    d = placed - xw[k]
-                    d -= box * np.round(d / box)
-                    if np.min(np.einsum("ij,ij->i", d, d)) < 9.0:
-                        ok = False
-                        break
-                if not ok:
-                    continue
-            placed = np.concatenate([placed, xw])
+            if clash(xw):
+                continue
+            for p in xw:
+                k = tuple(np.floor(p / cell).astype(int) % m)
+                grid.setdefault(k, []).append(p)
             out.append(xw)
             break
         else:
