@@ -123,7 +123,11 @@ struct isspa_engine {
     template <typename T>
     T *upload(const std::vector<T> &v) {
         T *p = alloc<T>(v.size());
-        if (!v.empty()) ck(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+        // complete before return: later launches go to non-blocking streams
+        if (!v.empty()) {
+            ck(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+            ck(cudaStreamSynchronize(0));
+        }
         return p;
     }
     template <typename T>
@@ -900,11 +904,14 @@ int isspa_set_tables(isspa_engine *e, const float *g_table, const float *e_table
         std::vector<float2> ftab, ljab;
         pack_isspa_tables(nt, e->n_g, e->n_e, e->n_f, e->g_raw_h, e->e_raw_h, e->f_raw_h, gtab, ftab);
         expand_lj(nlj, e->nbp_h, e->lj_ab_h, ljab);
+        // ordered on the engine's non-blocking stream, before any later launch
         ck(cudaStreamSynchronize(e->stream));
-        ck(cudaMemcpy(e->gtab, gtab.data(), sizeof(float4) * gtab.size(), cudaMemcpyHostToDevice));
-        ck(cudaMemcpy(e->ftab, ftab.data(), sizeof(float2) * ftab.size(), cudaMemcpyHostToDevice));
-        ck(cudaMemcpy(e->ljab, ljab.data(), sizeof(float2) * ljab.size(), cudaMemcpyHostToDevice));
-        ck(cudaMemcpy(e->g_raw, e->g_raw_h.data(), sizeof(float) * e->g_raw_h.size(), cudaMemcpyHostToDevice));
+        ck(cudaMemcpyAsync(e->gtab, gtab.data(), sizeof(float4) * gtab.size(), cudaMemcpyHostToDevice, e->stream));
+        ck(cudaMemcpyAsync(e->ftab, ftab.data(), sizeof(float2) * ftab.size(), cudaMemcpyHostToDevice, e->stream));
+        ck(cudaMemcpyAsync(e->ljab, ljab.data(), sizeof(float2) * ljab.size(), cudaMemcpyHostToDevice, e->stream));
+        ck(cudaMemcpyAsync(e->g_raw, e->g_raw_h.data(), sizeof(float) * e->g_raw_h.size(), cudaMemcpyHostToDevice,
+                           e->stream));
+        ck(cudaStreamSynchronize(e->stream));
     });
 }
 
@@ -936,15 +943,20 @@ int isspa_adjoint_mean_force(isspa_engine *e, int n_frames, const float *frames,
             e->adj_off = e->alloc<int>(W + 1);
             e->adj_atoms = e->alloc<int>(std::max<size_t>(1, e->bias_h.size()));
         }
-        ck(cudaMemcpy(saved.data(), e->pos, sizeof(float4) * N, cudaMemcpyDeviceToHost));
-        ck(cudaMemcpy(&saved_step, e->d_step, sizeof saved_step, cudaMemcpyDeviceToHost));
-        ck(cudaMemset(e->grads, 0, sizeof(double) * (size_t)W * per_w));
+        // Every copy below is ordered on the engine's (non-blocking) stream: a
+        // legacy-stream cudaMemcpy does not wait for the previous frame's
+        // adjoint kernels, and would overwrite positions and weights under them.
+        ck(cudaStreamSynchronize(e->stream));
+        ck(cudaMemcpyAsync(saved.data(), e->pos, sizeof(float4) * N, cudaMemcpyDeviceToHost, e->stream));
+        ck(cudaMemcpyAsync(&saved_step, e->d_step, sizeof saved_step, cudaMemcpyDeviceToHost, e->stream));
+        ck(cudaMemsetAsync(e->grads, 0, sizeof(double) * (size_t)W * per_w, e->stream));
+        ck(cudaStreamSynchronize(e->stream));
         std::vector<double> Jw(W, 0.0), cvec(3 * (size_t)N), facc(3 * (size_t)N);
         std::vector<long long> acc(3 * (size_t)N);
         for (int f = 0; f < n_frames; ++f) {
             const float4 *X = frames ? reinterpret_cast<const float4 *>(frames) + (size_t)f * N : saved.data();
-            if (frames) ck(cudaMemcpy(e->pos, X, sizeof(float4) * N, cudaMemcpyHostToDevice));
-            ck(cudaMemcpy(e->d_step, &steps[f], sizeof(uint32_t), cudaMemcpyHostToDevice));
+            if (frames) ck(cudaMemcpyAsync(e->pos, X, sizeof(float4) * N, cudaMemcpyHostToDevice, e->stream));
+            ck(cudaMemcpyAsync(e->d_step, &steps[f], sizeof(uint32_t), cudaMemcpyHostToDevice, e->stream));
             // weights c_i = +-n/2 on the two restraint groups of each window
             std::fill(cvec.begin(), cvec.end(), 0.0);
             std::vector<int> off(W + 1, 0), atoms;
@@ -977,10 +989,11 @@ int isspa_adjoint_mean_force(isspa_engine *e, int n_frames, const float *frames,
                 }
             }
             off[W] = (int)atoms.size();
-            ck(cudaMemcpy(e->cvec, cvec.data(), sizeof(double) * cvec.size(), cudaMemcpyHostToDevice));
-            ck(cudaMemcpy(e->adj_off, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice));
+            ck(cudaMemcpyAsync(e->cvec, cvec.data(), sizeof(double) * cvec.size(), cudaMemcpyHostToDevice, e->stream));
+            ck(cudaMemcpyAsync(e->adj_off, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice, e->stream));
             if (!atoms.empty())
-                ck(cudaMemcpy(e->adj_atoms, atoms.data(), sizeof(int) * atoms.size(), cudaMemcpyHostToDevice));
+                ck(cudaMemcpyAsync(e->adj_atoms, atoms.data(), sizeof(int) * atoms.size(), cudaMemcpyHostToDevice,
+                                   e->stream));
             // the value: every non-restraint force of the frame, projected
             ck(cudaMemsetAsync(e->facc, 0, 3 * sizeof(unsigned long long) * N, e->stream));
             launch_bonded(e->bonded_args(1, 1, 1), e->stream);
@@ -1041,10 +1054,12 @@ int isspa_adjoint_mean_force(isspa_engine *e, int n_frames, const float *frames,
             a.sc14 = e->sc14;
             launch_adjoint(a, e->stream);
             ck(cudaGetLastError());
+            // the next frame rewrites cvec/off/atoms and the device positions
+            ck(cudaStreamSynchronize(e->stream));
         }
-        ck(cudaStreamSynchronize(e->stream));
         std::vector<double> g((size_t)W * per_w);
-        ck(cudaMemcpy(g.data(), e->grads, sizeof(double) * g.size(), cudaMemcpyDeviceToHost));
+        ck(cudaMemcpyAsync(g.data(), e->grads, sizeof(double) * g.size(), cudaMemcpyDeviceToHost, e->stream));
+        ck(cudaStreamSynchronize(e->stream));
         const double inv = 1.0 / n_frames;
         for (int w = 0; w < W; ++w) {
             if (J) J[w] = Jw[w] * inv;
@@ -1058,9 +1073,10 @@ int isspa_adjoint_mean_force(isspa_engine *e, int n_frames, const float *frames,
             }
         }
         // restore the engine's state
-        ck(cudaMemcpy(e->pos, saved.data(), sizeof(float4) * N, cudaMemcpyHostToDevice));
-        ck(cudaMemcpy(e->d_step, &saved_step, sizeof saved_step, cudaMemcpyHostToDevice));
-        ck(cudaMemset(e->facc, 0, 3 * sizeof(unsigned long long) * N));
+        ck(cudaMemcpyAsync(e->pos, saved.data(), sizeof(float4) * N, cudaMemcpyHostToDevice, e->stream));
+        ck(cudaMemcpyAsync(e->d_step, &saved_step, sizeof saved_step, cudaMemcpyHostToDevice, e->stream));
+        ck(cudaMemsetAsync(e->facc, 0, 3 * sizeof(unsigned long long) * N, e->stream));
+        ck(cudaStreamSynchronize(e->stream));
     });
     return rc;
 }
@@ -1273,9 +1289,16 @@ int isspa_synchronize(isspa_engine *e) {
 int isspa_device_status(isspa_engine *e, int reset) {
     int rc = guard(e);
     if (rc) return rc;
+    // the engine's streams are non-blocking: order the read (and the reset)
+    // after the kernels already queued on them
     int st = 0;
-    if (cudaMemcpy(&st, e->status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return ISSPA_ERR_CUDA;
-    if (reset) cudaMemset(e->status, 0, sizeof(int));
+    if (cudaStreamSynchronize(e->stream) != cudaSuccess ||
+        cudaMemcpyAsync(&st, e->status, sizeof(int), cudaMemcpyDeviceToHost, e->stream) != cudaSuccess ||
+        (reset && cudaMemsetAsync(e->status, 0, sizeof(int), e->stream) != cudaSuccess) ||
+        cudaStreamSynchronize(e->stream) != cudaSuccess) {
+        cudaGetLastError();
+        return ISSPA_ERR_CUDA;
+    }
     if (st & kStatusNonFinite) return ISSPA_ERR_NONFINITE;
     if (st & kStatusOverflow) return ISSPA_ERR_OVERFLOW;
     if (st & kStatusBounds) return ISSPA_ERR_BOUNDS;
@@ -1358,7 +1381,8 @@ int isspa_set_mc_points(isspa_engine *e, const float *xyz, long long n) {
     if (rc) return rc;
     rc = run_guarded([&] {
         if (!e->pts_in) e->pts_in = e->alloc<float>(3 * (size_t)e->n_points);
-        ck(cudaMemcpy(e->pts_in, xyz, sizeof(float) * 3 * n, cudaMemcpyHostToDevice));
+        ck(cudaMemcpyAsync(e->pts_in, xyz, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, e->stream));
+        ck(cudaStreamSynchronize(e->stream));
     });
     if (!rc && !e->inject) {
         e->inject = true;

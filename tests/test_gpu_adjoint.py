@@ -87,3 +87,15 @@ def test_adjoint_theta_gradient_matches_central_differences(setup):
     print("dJ/dtheta fd ", np.round(fd, 6))
     print("normwise relative error", err)
     assert err < 1e-4
+
+
+def test_adjoint_repeat_calls_agree(setup):
+    """Consecutive multi-frame calls give the same J and gradients (FP64
+    atomics only reorder sums); each frame's uploads are ordered after the
+    previous frame's adjoint kernels."""
+    ff, wins, eng, frames, steps, per_window, th = setup
+    a = eng.adjoint_mean_force(steps, frames)
+    eng.step(3)
+    b = eng.adjoint_mean_force(steps, frames)
+    for x, y in zip(a, b):
+        assert np.abs(x - y).max() <= 1e-12 * max(np.abs(x).max(), 1e-300)
