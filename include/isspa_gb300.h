@@ -101,13 +101,17 @@ typedef struct isspa_system_desc {
 
 /* ---- engine options ------------------------------------------------------ */
 typedef struct isspa_engine_options {
-    int isspa_terms;     /* bit mask: 1 multipole, 2 tabulated LJ, 4 CDD; 0 => all (7) */
-    int nonbond_terms;   /* bit mask: 1 LJ, 2 Coulomb, 4 IS-SPA correction; 0 => all (7) */
+    int isspa_terms;     /* bit mask: 1 multipole, 2 tabulated LJ, 4 CDD; 0 => all (7);
+                            ISSPA_TERMS_NONE => no IS-SPA pass at all */
+    int nonbond_terms;   /* bit mask: 1 LJ, 2 Coulomb, 4 IS-SPA correction; 0 => all (7);
+                            ISSPA_TERMS_NONE => no nonbond pass at all */
     int use_graph;       /* isspa_step captures the step in a CUDA graph (default 1) */
     int field_split;     /* atom-loop split per MC point in the field kernel; 0 => auto */
     int force_chunk;     /* MC points per force-kernel work item; 0 => auto */
     size_t mem_cap;      /* device bytes the engine may allocate; 0 => unlimited */
 } isspa_engine_options;
+
+#define ISSPA_TERMS_NONE (-1)
 
 typedef struct isspa_engine isspa_engine;
 typedef struct isspa_host_system isspa_host_system;
@@ -254,6 +258,39 @@ int isspa_set_tables(isspa_engine *e, const float *g_table, const float *e_table
  * NULL. */
 int isspa_adjoint_mean_force(isspa_engine *e, int n_frames, const float *frames, const uint32_t *steps,
                              double *J, double *dJ_df, double *dJ_dg, double *dJ_dA, double *dJ_dB);
+
+/* ---- energies and virial (no counterpart in the reference, which reports
+ * none) ------------------------------------------------------------------- */
+/* Components of isspa_energies, kcal/mol, per window:
+ *   KIN_BEFORE  sum m v^2/2 with the stored half-step velocities v(t-dt/2);
+ *   KIN_AFTER   the same with v(t+dt/2) = v(t-dt/2) + F(t) dt/m, the
+ *               thermostat-free leapfrog kick (leapfrog_cuda.cu:57-60);
+ *               the kinetic energy at t is their mean;
+ *   BOND        sum k (r - r0)^2           (bond_force_cuda.cu:36-50, 2k stored)
+ *   ANGLE       sum k (theta - theta0)^2   (angle_force_cuda.cu:19-52)
+ *   DIHEDRAL    sum V (1 + cos(n phi - phase))   (dih_force_cuda.cu:86-135)
+ *   LJ14, COUL14  scaled 1-4 terms          (dih_force_cuda.cu:60-82)
+ *   LJ, COUL    A/r^12 - B/r^6 and q q / r over non-excluded pairs
+ *               (nonbond_force_cuda.cu:131-136)
+ *   CORR        the potential of the IS-SPA dielectric correction
+ *               (nonbond_force_cuda.cu:141-147), zero at infinity; it is the
+ *               pair potential of the force only when every IS-SPA type has
+ *               the same rmax (each ordered pair uses rmax of the partner)
+ *   UMBRELLA    k/2 (|COM0 - COM1| - x0)^2  (us_force_cuda.cu:14-48)
+ *   VIRIAL      sum r . F over the conservative terms above (pair, bonded
+ *               and restraint forces); the IS-SPA mean-field force has no
+ *               potential and is in neither the energy nor the virial.
+ * Each term follows the engine's term options.  Pair energies are evaluated
+ * in FP32 like the forces; every reduction is in FP64. */
+enum { ISSPA_E_KIN_BEFORE = 0, ISSPA_E_KIN_AFTER, ISSPA_E_BOND, ISSPA_E_ANGLE, ISSPA_E_DIHEDRAL,
+       ISSPA_E_LJ14, ISSPA_E_COUL14, ISSPA_E_LJ, ISSPA_E_COUL, ISSPA_E_CORR, ISSPA_E_UMBRELLA,
+       ISSPA_E_VIRIAL, ISSPA_E_COUNT };
+/* Energies of the engine's current state: computes the forces of the current
+ * step (every enabled term, MC points of the current step counter) into the
+ * accumulator, reduces the components above into out[n_windows][ISSPA_E_COUNT]
+ * and clears the accumulator again.  Positions, velocities and the step
+ * counter are not changed, so isspa_step continues the same trajectory. */
+int isspa_energies(isspa_engine *e, double *out);
 
 /* ---- neighbour and cell lists (neighborlist_cuda.cu, cell_list_cuda.cu) -- */
 /* All-pairs neighbour list of window 0 with r^2 < rnn^2, exclusions as the

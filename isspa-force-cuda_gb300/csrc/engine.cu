@@ -87,6 +87,7 @@ struct isspa_engine {
     double *cvec = nullptr, *lam = nullptr, *grads = nullptr;
     int n_adj_cap = 0;
     double *com = nullptr, *cv = nullptr;
+    double *energy = nullptr;  // [n_windows][kECount], allocated on first use
     PointsDev pts{};
     float4 *raw_e = nullptr, *raw_e0 = nullptr;
     float *pts_in = nullptr;
@@ -244,7 +245,7 @@ struct isspa_engine {
         a.atype = atype;
         a.win = win;
         a.tiles = field_tiles;
-        a.n_tiles = n_field_tiles;
+        a.n_tiles = opt.isspa_terms ? n_field_tiles : 0;
         a.gtab = gtab;
         a.rmax = rmax;
         a.n_gbins = n_g - 1;
@@ -274,7 +275,7 @@ struct isspa_engine {
         a.win = win;
         a.items = force_items;
         a.chunks = force_chunks;
-        a.n_items = n_force_items;
+        a.n_items = opt.isspa_terms ? n_force_items : 0;
         a.pts = pts;
         a.ftab = ftab;
         a.rmax = rmax;
@@ -296,7 +297,7 @@ struct isspa_engine {
         a.win = win;
         a.items = nb_items;
         a.items_nj = nb_nj;
-        a.n_items = n_nb_items;
+        a.n_items = opt.nonbond_terms ? n_nb_items : 0;
         a.ljab = ljab;
         a.n_lj_types = n_lj_types;
         a.rmax = rmax;
@@ -347,6 +348,18 @@ struct isspa_engine {
         a.status = status;
         return a;
     }
+    StateEnergyArgs state_energy_args() const {
+        StateEnergyArgs a{};
+        a.vel = vel;
+        a.facc = facc;
+        a.atom_win = atom_win;
+        a.win = win;
+        a.n_atoms = n_atoms;
+        a.us_windows = us_windows;
+        a.n_us_windows = n_us;
+        a.cv = cv;
+        return a;
+    }
     LeapfrogArgs leapfrog_args() const {
         LeapfrogArgs a{};
         a.pos = pos;
@@ -379,9 +392,9 @@ struct isspa_engine {
     // Which kernels a step launches (the wrappers skip empty work lists).
     bool launches(int k) const {
         switch (k) {
-            case ISSPA_K_FIELD: return n_field_tiles > 0;
-            case ISSPA_K_FORCE: return n_force_items > 0;
-            case ISSPA_K_NONBOND: return n_nb_items > 0;
+            case ISSPA_K_FIELD: return opt.isspa_terms && n_field_tiles > 0;
+            case ISSPA_K_FORCE: return opt.isspa_terms && n_force_items > 0;
+            case ISSPA_K_NONBOND: return opt.nonbond_terms && n_nb_items > 0;
             case ISSPA_K_BONDED: return n_bonds + n_angles + n_dihs > 0;
             case ISSPA_K_UMBRELLA: return n_us > 0;
             case ISSPA_K_LEAPFROG: return n_atoms > 0;
@@ -839,8 +852,11 @@ int isspa_engine_create(const isspa_system_desc *windows, int n_windows, const i
     }
     if (opt) e->opt = *opt;
     else isspa_default_options(&e->opt);
-    if (e->opt.isspa_terms == 0) e->opt.isspa_terms = 7;
-    if (e->opt.nonbond_terms == 0) e->opt.nonbond_terms = 7;
+    // 0 selects every term; ISSPA_TERMS_NONE switches the pass off (mask 0)
+    if (e->opt.isspa_terms < 0) e->opt.isspa_terms = 0;
+    else if (e->opt.isspa_terms == 0) e->opt.isspa_terms = 7;
+    if (e->opt.nonbond_terms < 0) e->opt.nonbond_terms = 0;
+    else if (e->opt.nonbond_terms == 0) e->opt.nonbond_terms = 7;
     if (cudaGetDevice(&e->device) != cudaSuccess) {
         cudaGetLastError();
         return ISSPA_ERR_CUDA;
@@ -920,6 +936,8 @@ int isspa_adjoint_mean_force(isspa_engine *e, int n_frames, const float *frames,
     if (!e || n_frames <= 0 || !steps) return ISSPA_ERR_ARG;
     int rc = guard(e);
     if (rc) return rc;
+    // the gradient kernels differentiate the full force (every term)
+    if ((e->opt.isspa_terms & 7) != 7 || (e->opt.nonbond_terms & 7) != 7) return ISSPA_ERR_STATE;
     const int W = e->n_windows, N = e->n_atoms;
     const long long P = e->n_points;
     const long long nF = (long long)e->n_itypes * e->n_f, nG = (long long)e->n_itypes * e->n_g;
@@ -1077,6 +1095,38 @@ int isspa_adjoint_mean_force(isspa_engine *e, int n_frames, const float *frames,
         ck(cudaMemcpyAsync(e->d_step, &saved_step, sizeof saved_step, cudaMemcpyHostToDevice, e->stream));
         ck(cudaMemsetAsync(e->facc, 0, 3 * sizeof(unsigned long long) * N, e->stream));
         ck(cudaStreamSynchronize(e->stream));
+    });
+    return rc;
+}
+
+static_assert(kECount == ISSPA_E_COUNT && kEVirial == ISSPA_E_VIRIAL && kEUmbrella == ISSPA_E_UMBRELLA &&
+                  kELj == ISSPA_E_LJ && kEKinAfter == ISSPA_E_KIN_AFTER,
+              "energy slots must match the public enum");
+
+int isspa_energies(isspa_engine *e, double *out) {
+    if (!e || !out) return ISSPA_ERR_ARG;
+    int rc = guard(e);
+    if (rc) return rc;
+    rc = run_guarded([&] {
+        const size_t ne = (size_t)e->n_windows * kECount;
+        if (!e->energy) e->energy = e->alloc<double>(ne);
+        cudaStream_t s = e->stream;
+        ck(cudaStreamSynchronize(s));
+        ck(cudaMemsetAsync(e->facc, 0, 3 * sizeof(unsigned long long) * e->n_atoms, s));
+        ck(cudaMemsetAsync(e->energy, 0, sizeof(double) * ne, s));
+        // the forces of the current step, in the reference order
+        launch_bonded(e->bonded_args(1, 1, 1), s);
+        e->enqueue_isspa(s);
+        launch_nonbond(e->nonbond_args(), s);
+        launch_umbrella(e->umbrella_args(), s);
+        // energies of the same configuration, and the kick the forces give
+        launch_nonbond_energy(e->nonbond_args(), e->energy, s);
+        launch_bonded_energy(e->bonded_args(1, 1, 1), e->energy, s);
+        launch_state_energy(e->state_energy_args(), e->energy, s);
+        ck(cudaGetLastError());
+        ck(cudaMemcpyAsync(out, e->energy, sizeof(double) * ne, cudaMemcpyDeviceToHost, s));
+        ck(cudaMemsetAsync(e->facc, 0, 3 * sizeof(unsigned long long) * e->n_atoms, s));
+        ck(cudaStreamSynchronize(s));
     });
     return rc;
 }

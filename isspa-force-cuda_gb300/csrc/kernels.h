@@ -169,6 +169,26 @@ struct AdjointArgs {
     const float2 *sc14;
 };
 
+// ---- energies and virial (FP64 reductions) ----------------------------------
+// Component slots, identical to the ISSPA_E_* enum of the public header.
+enum EnergySlot {
+    kEKinBefore = 0, kEKinAfter, kEBond, kEAngle, kEDihedral, kELj14, kECoul14, kELj, kECoul, kECorr,
+    kEUmbrella, kEVirial, kECount
+};
+struct StateEnergyArgs {
+    const float4 *vel;                 // v(t - dt/2), mass in .w
+    const unsigned long long *facc;    // F(t), fixed point
+    const int *atom_win;
+    const WinDev *win;
+    int n_atoms;
+    const int *us_windows;             // restrained windows and their CV
+    int n_us_windows;
+    const double *cv;
+};
+void launch_nonbond_energy(const NonbondArgs &a, double *energy, cudaStream_t s);
+void launch_bonded_energy(const BondedArgs &a, double *energy, cudaStream_t s);
+void launch_state_energy(const StateEnergyArgs &a, double *energy, cudaStream_t s);
+
 void launch_adjoint(const AdjointArgs &a, cudaStream_t s);
 void launch_field(const FieldArgs &a, int split, bool raw, cudaStream_t s);
 void launch_force(const ForceArgs &a, cudaStream_t s);

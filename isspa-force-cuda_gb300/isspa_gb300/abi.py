@@ -74,6 +74,11 @@ class NoallocInputs(C.Structure):
 
 
 NOALLOC_SCRATCH_BYTES = 16 << 20
+TERMS_NONE = -1  # ISSPA_TERMS_NONE: switches the IS-SPA or nonbond pass off
+
+# isspa_energies components (the ISSPA_E_* enum), kcal/mol
+ENERGY_NAMES = ("kin_before", "kin_after", "bond", "angle", "dihedral", "lj14", "coul14", "lj", "coul",
+                "corr", "umbrella", "virial")
 
 # (name, restype, argtypes); every exported entry point of include/isspa_gb300.h
 _P = C.c_void_p
@@ -126,6 +131,7 @@ SIGNATURES = [
     ("isspa_get_point_fields", C.c_int, [_P, _P, _P, _P, _P, _P, C.c_longlong]),
     ("isspa_set_tables", C.c_int, [_P, _P, _P, _P, _P]),
     ("isspa_adjoint_mean_force", C.c_int, [_P, C.c_int, _P, _P, _P, _P, _P, _P, _P]),
+    ("isspa_energies", C.c_int, [_P, _P]),
     ("isspa_neighbor_list", C.c_int, [_P, C.c_float, C.c_int, _P, _P]),
     ("isspa_cell_list", C.c_int, [_P, C.c_float, _P, _P]),
     ("isspa_measure_fp32_peak", C.c_int, [C.POINTER(C.c_double)]),

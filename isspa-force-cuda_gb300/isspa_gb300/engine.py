@@ -230,6 +230,13 @@ class Engine:
                                                      _ptr(J), _ptr(df), _ptr(dg), _ptr(dA), _ptr(dB)), "adjoint")
         return J, df, dg, dA, dB
 
+    def energies(self) -> np.ndarray:
+        """Energy components of the current state per window, FP64 kcal/mol,
+        [n_windows][len(abi.ENERGY_NAMES)] (state unchanged)."""
+        out = np.zeros((self.n_windows, len(abi.ENERGY_NAMES)))
+        abi.check(abi.lib().isspa_energies(self._h, _ptr(out)), "energies")
+        return out
+
     # --------------------------------------------------------------- lists
     def neighbor_list(self, rnn: float, max_per_atom: int = 576):
         n = self.windows[0].n_atoms

@@ -817,3 +817,174 @@ double orc_adjoint(const orc_isspa_sys *s, const orc_nb_sys *nb, int n_mc, const
     free(w); free(cnt); free(E); free(E0); free(lam);
     return J;
 }
+
+/* ---------------------------------------------------------------------------
+ * Energies and virial of one window (the potentials whose negative gradients
+ * are the forces above), FP64 values from the float geometry:
+ *   out[0], out[1]  kinetic m v^2/2 with v(t-dt/2) and with the
+ *                   thermostat-free kick v + F dt/m (leapfrog_cuda.cu:57-60,
+ *                   float arithmetic as the integrator);
+ *   out[2..4]       bond k(r-r0)^2, angle k(theta-theta0)^2 (2k stored),
+ *                   dihedral V(1+cos(n phi - phase));
+ *   out[5], out[6]  scaled 1-4 LJ and Coulomb;
+ *   out[7..9]       pair LJ, Coulomb, IS-SPA correction (nonbond_force_cuda.cu:
+ *                   131-147; correction integrated from infinity with the
+ *                   partner's rmax, ordered pairs halved);
+ *   out[10]         umbrella k/2 (d - x0)^2;
+ *   out[11]         virial sum r . F over those terms.
+ * ------------------------------------------------------------------------- */
+void orc_energies(const orc_nb_sys *s, int nb_terms, int n_bonds, const int *bond_atoms,
+                  const float *bond_params, int n_angles, const int *angle_atoms,
+                  const float *angle_params, int nd, const int *dih_atoms, const int *dih_types,
+                  const float *dih_params, const float *scaled14, int nbias, const int *bias_list,
+                  const float *mfrac, double us_k, double us_x0, const float *vel, const double *f,
+                  float dt, double out[12]) {
+    const int N = s->n_atoms;
+    const float *pos = s->pos;
+    const float L = s->box, h = 0.5f * s->box;
+    const double epf = 1.0 - 1.0 / (double)ORC_EP;
+    for (int k = 0; k < 12; ++k) out[k] = 0.0;
+    double elj = 0.0, ec = 0.0, ecr = 0.0, vir = 0.0;
+#pragma omp parallel for schedule(dynamic, 4) reduction(+ : elj, ec, ecr, vir)
+    for (int i = 0; i < N; ++i) {
+        const float *xi = pos + 4 * i;
+        for (int j = 0; j < N; ++j) {
+            if (j == i) continue;
+            const float *xj = pos + 4 * j;
+            const float rx = mimg(xi[0] - xj[0], L, h);
+            const float ry = mimg(xi[1] - xj[1], L, h);
+            const float rz = mimg(xi[2] - xj[2], L, h);
+            const float d2 = dist2f(rx, ry, rz);
+            const double dd2 = (double)rx * rx + (double)ry * ry + (double)rz * rz, dd = sqrt(dd2);
+            const double qq = (double)xi[3] * (double)xj[3];
+            const float rmj = s->rmax[s->isspa_type[j]];
+            const float two = 2.0f * rmj;
+            if (nb_terms & ORC_NB_CORR) {
+                if (d2 > two * two) {
+                    const double u = -2.0 * qq * epf / (3.0 * dd);
+                    ecr += u;
+                    vir += u;
+                } else {
+                    const double rm = rmj, r4 = rm * rm * rm * rm;
+                    ecr += qq * epf * ((4.0 * rm * dd2 - dd2 * dd) / (24.0 * r4) - 2.0 / (3.0 * rm));
+                    vir += -qq * epf * (8.0 * rm - 3.0 * dd) * dd2 / (24.0 * r4);
+                }
+            }
+            if (!orc_excluded(s, i, j)) {
+                if (nb_terms & ORC_NB_LJ) {
+                    const int nlj = s->nb_parm_index[s->n_types * s->lj_type[i] + s->lj_type[j]];
+                    const double A = s->lj_ab[2 * nlj], B = s->lj_ab[2 * nlj + 1];
+                    const double r6 = 1.0 / (dd2 * dd2 * dd2);
+                    elj += r6 * (A * r6 - B);
+                    vir += r6 * (12.0 * A * r6 - 6.0 * B);
+                }
+                if (nb_terms & ORC_NB_COUL) {
+                    ec += qq / dd;
+                    vir += qq / dd;
+                }
+            }
+        }
+    }
+    out[7] = 0.5 * elj;
+    out[8] = 0.5 * ec;
+    out[9] = 0.5 * ecr;
+    out[11] = 0.5 * vir;
+    for (int b = 0; b < n_bonds; ++b) {
+        const int x = bond_atoms[3 * b], y = bond_atoms[3 * b + 1], t = bond_atoms[3 * b + 2];
+        double r[3];
+        rvec(pos, x, y, L, h, r);
+        const double d = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]), dr = d - bond_params[2 * t + 1];
+        out[2] += 0.5 * bond_params[2 * t] * dr * dr;
+        out[11] += -(double)bond_params[2 * t] * dr * d;
+    }
+    for (int a = 0; a < n_angles; ++a) {
+        const int x = angle_atoms[4 * a], y = angle_atoms[4 * a + 1], z = angle_atoms[4 * a + 2],
+                  t = angle_atoms[4 * a + 3];
+        double r1[3], r2[3];
+        rvec(pos, x, y, L, h, r1);
+        rvec(pos, y, z, L, h, r2);
+        const double c11 = r1[0] * r1[0] + r1[1] * r1[1] + r1[2] * r1[2];
+        const double c22 = r2[0] * r2[0] + r2[1] * r2[1] + r2[2] * r2[2];
+        const double c12 = r1[0] * r2[0] + r1[1] * r2[1] + r1[2] * r2[2];
+        const double b = -c12 / sqrt(c11 * c22);
+        const double theta = b >= 1.0 ? 1.0e-16 : (b <= -1.0 ? (double)ORC_PI : acos(b));
+        const double dt_ = theta - angle_params[2 * t + 1];
+        out[3] += 0.5 * angle_params[2 * t] * dt_ * dt_;
+        const double fa = angle_params[2 * t] * dt_ / sqrt(c11 * c22 - c12 * c12);
+        for (int k = 0; k < 3; ++k) {
+            const double fx = fa * (c12 / c11 * r1[k] - r2[k]), fz = fa * (r1[k] - c12 / c22 * r2[k]);
+            out[11] += r1[k] * fx - r2[k] * fz;
+        }
+    }
+    for (int d = 0; d < nd; ++d) {
+        int ax = dih_atoms[4 * d], ay = dih_atoms[4 * d + 1], az = dih_atoms[4 * d + 2], aw = dih_atoms[4 * d + 3];
+        const int t = dih_types[d];
+        if (az > 0 && aw > 0) {
+            const int nlj = s->nb_parm_index[s->n_types * s->lj_type[ax] + s->lj_type[aw]];
+            const double A = s->lj_ab[2 * nlj], B = s->lj_ab[2 * nlj + 1];
+            double r14[3];
+            rvec(pos, ax, aw, L, h, r14);
+            const double rm = r14[0] * r14[0] + r14[1] * r14[1] + r14[2] * r14[2];
+            const double r6 = 1.0 / (rm * rm * rm);
+            const double uc = (double)pos[4 * ax + 3] * pos[4 * aw + 3] / (sqrt(rm) * scaled14[2 * t]);
+            out[5] += r6 * (A * r6 - B) / scaled14[2 * t + 1];
+            out[6] += uc;
+            out[11] += r6 * (12.0 * A * r6 - 6.0 * B) / scaled14[2 * t + 1] + uc;
+        }
+        if (aw < 0) aw = -aw;
+        if (az < 0) az = -az;
+        double r12[3], r23[3], r34[3];
+        rvec(pos, ax, ay, L, h, r12);
+        rvec(pos, ay, az, L, h, r23);
+        rvec(pos, az, aw, L, h, r34);
+        const double c11 = r12[0] * r12[0] + r12[1] * r12[1] + r12[2] * r12[2];
+        const double c22 = r23[0] * r23[0] + r23[1] * r23[1] + r23[2] * r23[2];
+        const double c12 = r12[0] * r23[0] + r12[1] * r23[1] + r12[2] * r23[2];
+        const double c33 = r34[0] * r34[0] + r34[1] * r34[1] + r34[2] * r34[2];
+        const double c23 = r23[0] * r34[0] + r23[1] * r34[1] + r23[2] * r34[2];
+        const double c13 = r12[0] * r34[0] + r12[1] * r34[1] + r12[2] * r34[2];
+        const double t1 = c13 * c22 - c12 * c23, t2 = c11 * c23 - c12 * c13, t3 = c12 * c12 - c11 * c22;
+        const double t4 = c22 * c33 - c23 * c23, t5 = c13 * c23 - c12 * c33, t6 = -t1;
+        const double bb = sqrt(-t3 * t4), a = t6 / bb;
+        const float *pr = dih_params + 4 * t;
+        double fd = 0.0, phi = a <= -1.0 ? (double)ORC_PI : 0.0;
+        if (a > -1.0 && a < 1.0) {
+            phi = acos(a);
+            fd = pr[0] * pr[1] * sin(pr[0] * phi - pr[2]) * c22 / (sin(phi) * bb);
+        }
+        out[4] += pr[1] * (1.0 + cos(pr[0] * phi - pr[2]));
+        for (int k = 0; k < 3; ++k) {
+            const double f1 = fd / t3 * (t1 * r12[k] + t2 * r23[k] + t3 * r34[k]);
+            const double f4 = -fd / t4 * (t4 * r12[k] + t5 * r23[k] + t6 * r34[k]);
+            const double f3 = c12 / c22 * f1 - (1.0 + c23 / c22) * f4;
+            out[11] += r12[k] * f1 - r23[k] * f3 - (r23[k] + r34[k]) * f4;
+        }
+    }
+    if (nbias > 0) {
+        double com[6];
+        double *fs = (double *)calloc(3 * (size_t)N, sizeof(double));
+        orc_us(nbias, bias_list, mfrac, us_k, us_x0, pos, s->box, fs, com);
+        free(fs);
+        double r[3];
+        for (int k = 0; k < 3; ++k) {
+            r[k] = com[k] - com[3 + k];
+            if (r[k] > 0.5 * s->box) r[k] -= s->box;
+            else if (r[k] < -0.5 * s->box) r[k] += s->box;
+        }
+        const double dist = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]), dx = dist - us_x0;
+        out[10] = 0.5 * us_k * dx * dx;
+        out[11] += -us_k * dx * dist;
+    }
+    for (int i = 0; i < N; ++i) {
+        const float m = vel[4 * i + 3], k = dt / m;
+        double kb = 0.0, ka = 0.0;
+        for (int d = 0; d < 3; ++d) {
+            const float v = vel[4 * i + d];
+            const float vp = fmaf((float)f[3 * i + d], k, v);
+            kb += (double)v * v;
+            ka += (double)vp * vp;
+        }
+        out[0] += 0.5 * (double)m * kb;
+        out[1] += 0.5 * (double)m * ka;
+    }
+}

@@ -145,6 +145,18 @@ double orc_adjoint(const orc_isspa_sys *s, const orc_nb_sys *nb, int n_mc, const
                    const float *scaled14, double *dJ_df, double *dJ_dg, double *dJ_dA,
                    double *dJ_dB);
 
+/* Energy components and virial of one window, FP64 (order of the engine's
+ * ISSPA_E_* enum): kinetic before/after the kick, bond, angle, dihedral,
+ * 1-4 LJ, 1-4 Coulomb, pair LJ, pair Coulomb, IS-SPA correction, umbrella,
+ * virial.  vel [N][4] (v, mass); f [N][3] the step's total force; dt the
+ * internal time step.  nbias = 0 skips the umbrella term. */
+void orc_energies(const orc_nb_sys *s, int nb_terms, int n_bonds, const int *bond_atoms,
+                  const float *bond_params, int n_angles, const int *angle_atoms,
+                  const float *angle_params, int nd, const int *dih_atoms, const int *dih_types,
+                  const float *dih_params, const float *scaled14, int nbias, const int *bias_list,
+                  const float *mfrac, double us_k, double us_x0, const float *vel, const double *f,
+                  float dt, double out[12]);
+
 #ifdef __cplusplus
 }
 #endif

@@ -195,6 +195,32 @@ class Oracle:
                             int(with_14), _p(f))
         return f
 
+    ENERGY_NAMES = ("kin_before", "kin_after", "bond", "angle", "dihedral", "lj14", "coul14", "lj", "coul",
+                    "corr", "umbrella", "virial")
+
+    def energies(self, force, nb_terms: int = 7, with_us: bool = True) -> np.ndarray:
+        """FP64 energy components (ENERGY_NAMES order) of the system's state;
+        `force` [N][3] is the step's total force (for the kinetic energy after
+        the kick)."""
+        s = self.s
+        out = np.zeros(12)
+        ba = _i32(s.bond_atoms if len(s.bond_atoms) else np.zeros((1, 3))); bp = _f32(s.bond_params)
+        aa = _i32(s.angle_atoms if len(s.angle_atoms) else np.zeros((1, 4))); ap = _f32(s.angle_params)
+        da = _i32(s.dih_atoms if len(s.dih_atoms) else np.zeros((1, 4)))
+        dt = _i32(s.dih_types if len(s.dih_types) else np.zeros(1))
+        dp = _f32(s.dih_params if len(s.dih_params) else np.zeros((1, 4)))
+        sc = _f32(s.scaled14 if len(s.scaled14) else np.ones((1, 2)))
+        us = with_us and bool(s.us_on)
+        bl = _i32(s.bias_list if us else np.zeros((1, 2)))
+        mf = _f32(s.bias_mass_fraction() if us else np.zeros(1))
+        vel = _f32(s.vel).reshape(-1, 4)
+        fo = np.ascontiguousarray(force, dtype=np.float64).reshape(-1, 3)
+        lib().orc_energies(C.byref(self.nsys), int(nb_terms), len(s.bond_atoms), _p(ba), _p(bp),
+                           len(s.angle_atoms), _p(aa), _p(ap), len(s.dih_atoms), _p(da), _p(dt), _p(dp),
+                           _p(sc), len(bl) if us else 0, _p(bl), _p(mf), C.c_double(float(s.us_k) if us else 0.0),
+                           C.c_double(float(s.us_x0) if us else 0.0), _p(vel), _p(fo), C.c_float(s.dt), _p(out))
+        return out
+
     def us(self):
         s = self.s
         f = np.zeros((self.n, 3))
