@@ -129,23 +129,28 @@ def ncu_traffic(kernel: str):
     return d.get(kernel)
 
 
-def cpu_oracle_rate(system, budget_s: float, min_steps: int = 1, max_steps: int = 1000000):
-    """Full force evaluations + leapfrog of the oracle on all host cores."""
+def cpu_oracle_rate(system, budget_s: float, min_steps: int = 1, max_steps: int = 1000000, gpu_force=None):
+    """Full force evaluations + leapfrog of the oracle on all host cores.  With
+    `gpu_force` (the engine's total force of step 0 on the same state) the
+    first oracle step also checks it: normwise max |dF| / max |F|."""
     import oracle
 
     oracle.build()
     cores = host_cores()
     o = oracle.Oracle(system, threads=cores)
+    err = None
     t0 = time.perf_counter()
     n = 0
     while n < max_steps:
         f, _, _ = o.total_force(seed=system.seed, step=n)
+        if n == 0 and gpu_force is not None:
+            err = float(np.abs(np.asarray(gpu_force)[:, :3] - f).max() / np.abs(f).max())
         o.leapfrog(f, seed=system.seed, step=n)
         n += 1
         if n >= min_steps and time.perf_counter() - t0 >= budget_s:
             break
     dt = time.perf_counter() - t0
-    return system.n_atoms * n / dt, n, dt, cores
+    return system.n_atoms * n / dt, n, dt, cores, err
 
 
 def run_gb300(args):
@@ -157,6 +162,8 @@ def run_gb300(args):
     N, M = sysm.n_atoms, sysm.n_mc
     P = N * M
     eng = ig.Engine(sysm)
+    f_step0 = eng.compute_forces()  # step-0 forces, checked against the oracle in the CPU leg
+    eng.zero_forces()
     shapes = eng.shapes() if args.no_autotune else eng.autotune()
     shapes["autotuned"] = not args.no_autotune
     eng.step(args.warmup)
@@ -220,7 +227,7 @@ def run_gb300(args):
                    "peak_source": "MEASURED_PEAKS.json" if pk else "fallback"}
     launches = int(sum(v[1] for v in kern.values()))
 
-    cpu_value, cpu_steps, cpu_s, cores = cpu_oracle_rate(sysm, budget_s=args.cpu_budget)
+    cpu_value, cpu_steps, cpu_s, cores, f_err = cpu_oracle_rate(sysm, budget_s=args.cpu_budget, gpu_force=f_step0)
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_step, 5), "higher_is_better": True,
@@ -240,6 +247,9 @@ def run_gb300(args):
                          "sample": f"{cpu_steps} full MD steps of the same 1100-atom system "
                                    f"({cpu_s:.1f} s), CPU oracle (FP64 values), OpenMP"},
         "device_status": status,
+        "force_error": {"normwise_vs_fp64_oracle": f_err, "target": 1e-5,
+                        "what": "total force of step 0 (bonded, IS-SPA, nonbond), same Philox MC points, "
+                                "max |F_gpu - F_oracle| / max |F_oracle|"},
     }
     clocks = clk.summary()
     line["clocks"] = clocks
@@ -281,7 +291,7 @@ def run_reference(args):
 
     sysm = synth.config_plain(seed=2)
     budget = args.cpu_budget * 3
-    value, n, dt, cores = cpu_oracle_rate(sysm, budget_s=budget, min_steps=1,
+    value, n, dt, cores, _ = cpu_oracle_rate(sysm, budget_s=budget, min_steps=1,
                                           max_steps=max(1, args.steps + args.warmup))
     line = {"impl": "reference", "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": 1,
             "steps": n, "warmup": 0, "ms_per_step": round(dt / n * 1e3, 3), "higher_is_better": True,

@@ -230,10 +230,15 @@ __global__ void __launch_bounds__(FieldShape<S>::kThreads) field_kernel(FieldArg
 
 // LJ = include the tabulated mean LJ force (term bit 2); the multipole and CDD
 // terms are shaped by the per-point constants of the field pass.
+// One MC point's records side by side in shared memory: a single base address
+// per point, the five float4 at immediate offsets (q3 / q4 picked per lane).
+struct alignas(16) PointRec {
+    float4 q[5];
+};
+
 template <bool LJ>
 __global__ void __launch_bounds__(kForceThreads, 10) force_kernel(ForceArgs a) {
-    __shared__ float4 s_q0[kForceThreads], s_q1[kForceThreads], s_q2[kForceThreads];
-    __shared__ float4 s_q3[kForceThreads], s_q4[kForceThreads];
+    __shared__ PointRec s_p[kForceThreads];
     const int4 item = a.items[blockIdx.x];
     const WinDev W = a.win[item.x];
     const int2 ch = a.chunks[item.w];
@@ -262,16 +267,17 @@ __global__ void __launch_bounds__(kForceThreads, 10) force_kernel(ForceArgs a) {
         __syncthreads();
         if (t < pn) {
             const long long pg = (long long)ch.x + p0 + t;
-            s_q0[t] = a.pts.q0[pg];
-            s_q1[t] = a.pts.q1[pg];
-            s_q2[t] = a.pts.q2[pg];
-            s_q3[t] = a.pts.q3[pg];
-            s_q4[t] = a.pts.q4[pg];
+            s_p[t].q[0] = a.pts.q0[pg];
+            s_p[t].q[1] = a.pts.q1[pg];
+            s_p[t].q[2] = a.pts.q2[pg];
+            s_p[t].q[3] = a.pts.q3[pg];
+            s_p[t].q[4] = a.pts.q4[pg];
         }
         __syncthreads();
 #pragma unroll 2
         for (int k = 0; k < pn; ++k) {
-            const float4 P = s_q0[k];
+            const float4 *R = s_p[k].q;
+            const float4 P = R[0];
             const float rx = mimg(P.x - xi.x, L, h);
             const float ry = mimg(P.y - xi.y, L, h);
             const float rz = mimg(P.z - xi.z, L, h);
@@ -281,9 +287,9 @@ __global__ void __launch_bounds__(kForceThreads, 10) force_kernel(ForceArgs a) {
             const float ri2 = ri * ri;
             const float ri3 = ri2 * ri;
             const float ri5 = ri3 * ri2;
-            const float4 E = s_q1[k];
-            const float4 K = s_q2[k];
-            const float4 D = (inside ? s_q3 : s_q4)[k];
+            const float4 E = R[1];
+            const float4 K = R[2];
+            const float4 D = R[inside ? 3 : 4];
             // multipole (:274-289) with the CDD term (:306-312) folded into D
             const float w = fmaf(E.x, rx, fmaf(E.y, ry, E.z * rz));
             const float dD = fmaf(D.x, rx, fmaf(D.y, ry, D.z * rz));

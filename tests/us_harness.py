@@ -9,10 +9,13 @@
 * `oracle_cv_series`: the CV |COM0 - COM1| of every `every`-th step of an
   oracle MD run (IS-SPA, nonbond, bonded, restraint, leapfrog + Andersen),
   with the engine's Philox keys.
-* `block_stats`, `mean_force_stats`, `umbrella_integration`: block-averaged
-  means and standard errors, the mean restraint force -k(<d> - x0) of a
-  window, and the free-energy profile from integrating the mean forces
-  between window means (trapezoids), with propagated errors.
+* `replica_stats`, `umbrella_integration`: the mean restraint force
+  -k(<d> - x0) of a window from independent replicas (each replica its own
+  Philox window index, so its own thermostat and MC-point streams); the
+  standard error comes from the spread of the replica means, which unlike
+  blocks of one run are uncorrelated (the CV relaxes over tens of ps).  Then
+  the free-energy profile from integrating the mean forces between window
+  means (trapezoids), with propagated errors.
 """
 from __future__ import annotations
 
@@ -23,10 +26,15 @@ import oracle as O
 
 K_US = 10.0
 X0S = (6.0, 8.0, 10.0, 12.0)
+REPLICAS = 8
 EQUIL_STEPS = 10_000
-PROD_STEPS = 100_000
+PROD_STEPS = 50_000
 EVERY = 10
-N_BLOCKS = 20
+
+
+def window_index(replica: int, window: int) -> int:
+    """Position of (replica, window) in the batched engine: replica-major."""
+    return replica * len(X0S) + window
 
 
 def window_system(x0: float, box: float = 80.0, seed: int = 1):
@@ -53,36 +61,28 @@ def _cv(com, box):
 
 
 def oracle_cv_series(s, n_steps: int, every: int, window: int = 0, threads: int = 1):
-    pos, vel = s.pos.copy(), s.vel.copy()
+    t = s.copy()
+    t.pos = np.ascontiguousarray(s.pos, np.float32).copy()
+    t.vel = np.ascontiguousarray(s.vel, np.float32).copy()
+    o = O.Oracle(t, threads=threads)  # reads o.pos / t.vel in place every call
     cv = []
     for k in range(n_steps):
-        t = s.copy()
-        t.pos, t.vel = pos, vel
-        o = O.Oracle(t, threads=threads)
         f, _, com = o.total_force(s.seed, k, window)
         po, vo, _ = o.leapfrog(f, s.seed, k, window)
         if (k + 1) % every == 0:
             cv.append(_cv(com, float(s.box)))
-        pos = pos.copy()
-        pos[:, :3] = po
-        vel = vel.copy()
-        vel[:, :3] = vo
         if not np.all(np.isfinite(po)):
             raise FloatingPointError(f"oracle run diverged at step {k}")
+        o.pos[:, :3] = po
+        t.vel[:, :3] = vo
     return np.asarray(cv)
 
 
-def block_stats(x, n_blocks: int = N_BLOCKS):
-    x = np.asarray(x, np.float64)
-    m = len(x) // n_blocks
-    blocks = x[: m * n_blocks].reshape(n_blocks, m).mean(1)
-    return float(blocks.mean()), float(blocks.std(ddof=1) / np.sqrt(n_blocks)), blocks
-
-
-def mean_force_stats(cv, x0: float, k: float = K_US):
-    m, se, blocks = block_stats(cv)
+def replica_stats(replica_means, x0: float, k: float = K_US):
+    r = np.asarray(replica_means, np.float64)
+    m, se = float(r.mean()), float(r.std(ddof=1) / np.sqrt(len(r)))
     return {"mean_cv": m, "se_cv": se, "mean_force": -k * (m - x0), "se_force": k * se,
-            "block_means": blocks.tolist()}
+            "replica_means": r.tolist()}
 
 
 def umbrella_integration(mean_cv, mean_force, se_force):
