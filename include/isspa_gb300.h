@@ -109,6 +109,7 @@ typedef struct isspa_engine_options {
     int field_split;     /* atom-loop split per MC point in the field kernel; 0 => auto */
     int force_chunk;     /* MC points per force-kernel work item; 0 => auto */
     size_t mem_cap;      /* device bytes the engine may allocate; 0 => unlimited */
+    int force_atoms_per_thread;  /* receiving atoms per IS-SPA force thread, 1 or 2; 0 => 1 */
 } isspa_engine_options;
 
 #define ISSPA_TERMS_NONE (-1)
@@ -162,14 +163,17 @@ int isspa_engine_info(const isspa_engine *e, int *n_windows, int *n_atoms_total,
 /* Launch shapes the engine chose (or was given) for its work lists:
  * shape[0] field atom-loop split, [1] field tiles, [2] force points per work
  * item, [3] force work items, [4] nonbond work items, [5] nonbond partners per
- * item, [6] SM count used for the choice. */
-int isspa_engine_shapes(const isspa_engine *e, int shape[7]);
-/* Autotuner: times every field-pass atom split and a set of force-pass chunk
- * lengths (those filling 1..6 whole waves of resident blocks, and powers of
- * two) on this engine's own workload with CUDA events (reps launches each),
- * keeps the fastest of each and reports the result as isspa_engine_shapes
- * does.  Clears the force accumulator; invalidates captured graphs. */
-int isspa_autotune(isspa_engine *e, int reps, int shape[7]);
+ * item, [6] SM count used for the choice, [7] receiving atoms per force
+ * thread. */
+#define ISSPA_SHAPE_COUNT 8
+int isspa_engine_shapes(const isspa_engine *e, int shape[ISSPA_SHAPE_COUNT]);
+/* Autotuner: times every field-pass atom split and, for 1 and 2 receiving
+ * atoms per force thread, a set of force-pass chunk lengths (those filling
+ * 1..6 whole waves of resident blocks, and powers of two) on this engine's own
+ * workload with CUDA events (reps launches each), keeps the fastest of each
+ * and reports the result as isspa_engine_shapes does.  Clears the force
+ * accumulator; invalidates captured graphs. */
+int isspa_autotune(isspa_engine *e, int reps, int shape[ISSPA_SHAPE_COUNT]);
 
 /* ---- per-step force calls (reference names and order) -------------------- */
 /* Each call adds its forces into the engine's force accumulator, exactly as the

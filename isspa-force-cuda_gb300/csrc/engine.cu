@@ -65,6 +65,7 @@ struct isspa_engine {
     int4 *force_items = nullptr;
     int2 *force_chunks = nullptr;
     int n_force_items = 0, force_chunk = 0;
+    int force_apt = 1;  // receiving atoms per force-kernel thread (1 or 2)
     int4 *nb_items = nullptr;
     int *nb_nj = nullptr;
     int n_nb_items = 0, nb_chunk = 0, n_sms = 0;
@@ -175,7 +176,7 @@ struct isspa_engine {
         return S;
     }
     int default_force_chunk() const {
-        const long long slots = (long long)n_sms * std::max(1, force_blocks_per_sm());
+        const long long slots = (long long)n_sms * std::max(1, force_blocks_per_sm(force_apt));
         double best = -1.0;
         int C = 64;
         for (long long c = 8192; c >= 64; --c) {  // longest chunk (fewest atomics) at equal efficiency
@@ -285,6 +286,7 @@ struct isspa_engine {
         a.f_dr = f_dr;
         a.f_inv = 1.0f / f_dr;
         a.terms = opt.isspa_terms;
+        a.atoms_per_thread = force_apt;
         a.facc = facc;
         a.status = status;
         return a;
@@ -683,6 +685,7 @@ void build(isspa_engine &E, const std::vector<isspa_host_system> &ws) {
     int S = E.opt.field_split;
     if (S != 1 && S != 2 && S != 4 && S != 8 && S != 16) S = E.default_field_split();
     E.set_field_split(S);
+    E.force_apt = E.opt.force_atoms_per_thread == 2 ? 2 : 1;
     E.set_force_chunk(E.opt.force_chunk > 0 ? E.opt.force_chunk : E.default_force_chunk());
     // nonbond items: 128 i-atoms x J partners
     std::vector<int4> nitems;
@@ -890,7 +893,7 @@ int isspa_engine_info(const isspa_engine *e, int *nw, int *na, long long *np) {
     return ISSPA_OK;
 }
 
-int isspa_engine_shapes(const isspa_engine *e, int shape[7]) {
+int isspa_engine_shapes(const isspa_engine *e, int shape[ISSPA_SHAPE_COUNT]) {
     if (!e || !shape) return ISSPA_ERR_ARG;
     shape[0] = e->field_split;
     shape[1] = e->n_field_tiles;
@@ -899,6 +902,7 @@ int isspa_engine_shapes(const isspa_engine *e, int shape[7]) {
     shape[4] = e->n_nb_items;
     shape[5] = e->nb_chunk;
     shape[6] = e->n_sms;
+    shape[7] = e->force_apt;
     return ISSPA_OK;
 }
 
@@ -1131,7 +1135,7 @@ int isspa_energies(isspa_engine *e, double *out) {
     return rc;
 }
 
-int isspa_autotune(isspa_engine *e, int reps, int shape[7]) {
+int isspa_autotune(isspa_engine *e, int reps, int shape[ISSPA_SHAPE_COUNT]) {
     int rc = guard(e);
     if (rc) return rc;
     if (reps <= 0) reps = 3;
@@ -1159,34 +1163,40 @@ int isspa_autotune(isspa_engine *e, int reps, int shape[7]) {
         }
         e->set_field_split(bestS);
         launch_field(e->field_args(), bestS, false, e->stream);
-        // force pass: chunk lengths that fill 1..6 whole waves, and powers of two
-        const long long slots = (long long)e->n_sms * std::max(1, force_blocks_per_sm());
+        // force pass: for 1 and 2 atoms per thread, the chunk lengths that fill
+        // 1..6 whole waves of that kernel's resident blocks, and powers of two
         long long maxP = 0;
         for (const WinDev &d : e->win_h) maxP = std::max(maxP, (long long)d.n_atoms * e->n_mc);
-        std::vector<int> cands = {e->default_force_chunk()};
-        for (int k = 1; k <= 6; ++k) {
-            long long lo = 64, hi = std::max<long long>(64, std::min<long long>(8192, maxP));
-            while (lo < hi) {  // smallest C with items <= k * slots
-                const long long mid = (lo + hi) / 2;
-                if (e->force_items_for(mid) <= k * slots) hi = mid;
-                else lo = mid + 1;
-            }
-            cands.push_back((int)lo);
-        }
-        for (int c : {128, 256, 512, 1024, 2048, 4096})
-            if (c <= std::max<long long>(128, maxP)) cands.push_back(c);
-        std::sort(cands.begin(), cands.end());
-        cands.erase(std::unique(cands.begin(), cands.end()), cands.end());
         best = 1e30f;
-        int bestC = e->force_chunk;
-        for (int c : cands) {
-            e->set_force_chunk(c);
-            const float ms = time_it([&] { launch_force(e->force_args(), e->stream); });
-            if (ms < best) {
-                best = ms;
-                bestC = c;
+        int bestC = e->force_chunk, bestA = e->force_apt;
+        for (int apt : {1, 2}) {
+            e->force_apt = apt;
+            const long long slots = (long long)e->n_sms * std::max(1, force_blocks_per_sm(apt));
+            std::vector<int> cands = {e->default_force_chunk()};
+            for (int k = 1; k <= 6; ++k) {
+                long long lo = 64, hi = std::max<long long>(64, std::min<long long>(8192, maxP));
+                while (lo < hi) {  // smallest C with items <= k * slots
+                    const long long mid = (lo + hi) / 2;
+                    if (e->force_items_for(mid) <= k * slots) hi = mid;
+                    else lo = mid + 1;
+                }
+                cands.push_back((int)lo);
+            }
+            for (int c : {128, 256, 512, 1024, 2048, 4096})
+                if (c <= std::max<long long>(128, maxP)) cands.push_back(c);
+            std::sort(cands.begin(), cands.end());
+            cands.erase(std::unique(cands.begin(), cands.end()), cands.end());
+            for (int c : cands) {
+                e->set_force_chunk(c);
+                const float ms = time_it([&] { launch_force(e->force_args(), e->stream); });
+                if (ms < best) {
+                    best = ms;
+                    bestC = c;
+                    bestA = apt;
+                }
             }
         }
+        e->force_apt = bestA;
         e->set_force_chunk(bestC);
         ck(cudaMemsetAsync(e->facc, 0, 3 * sizeof(unsigned long long) * e->n_atoms, e->stream));
         ck(cudaStreamSynchronize(e->stream));

@@ -228,106 +228,135 @@ __global__ void __launch_bounds__(FieldShape<S>::kThreads) field_kernel(FieldArg
     a.out.q4[pg] = make_float4(fmaf(a1, hx, cd * fx), fmaf(a1, hy, cd * fy), fmaf(a1, hz, cd * fz), 1.5f * a3);
 }
 
-// LJ = include the tabulated mean LJ force (term bit 2); the multipole and CDD
-// terms are shaped by the per-point constants of the field pass.
 // One MC point's records side by side in shared memory: a single base address
 // per point, the five float4 at immediate offsets (q3 / q4 picked per lane).
 struct alignas(16) PointRec {
     float4 q[5];
 };
 
-template <bool LJ>
-__global__ void __launch_bounds__(kForceThreads, 10) force_kernel(ForceArgs a) {
+// LJ = include the tabulated mean LJ force (term bit 2); the multipole and CDD
+// terms are shaped by the per-point constants of the field pass.  A = receiving
+// atoms per thread (t and t + 128/A of the item): each staged point's records
+// are read once from shared memory for A atoms.  Every atom sees the same
+// arithmetic in the same order whatever A is.
+template <int A>
+struct ForceShape {
+    static constexpr int kThreads = kForceThreads / A;
+    static constexpr int kMinBlocks = A == 1 ? 10 : 12;  // 48 / 85 registers per thread
+};
+
+template <bool LJ, int A>
+__global__ void __launch_bounds__(ForceShape<A>::kThreads, ForceShape<A>::kMinBlocks) force_kernel(ForceArgs a) {
+    constexpr int kT = ForceShape<A>::kThreads;
     __shared__ PointRec s_p[kForceThreads];
     const int4 item = a.items[blockIdx.x];
     const WinDev W = a.win[item.x];
     const int2 ch = a.chunks[item.w];
     const int t = threadIdx.x;
-    const bool active = t < item.z;
-    const int ai = item.y + (active ? t : 0);
-    const float4 xi = a.pos[ai];
-    const int ity = a.atype[ai].y;
-    const float rm = __ldg(a.rmax + ity);
-    const float rm2 = __fmul_rn(rm, rm);
-    const int frow = ity * a.n_f;
     const float L = W.box, h = W.hbox;
     const float f_r0 = a.f_r0, f_dr = a.f_dr, f_inv = a.f_inv;
     const int nf = a.n_f;
-
-    const float vt = __ldg(a.vtot + ity);
+    bool active[A];
+    int ai[A], frow[A];
+    float4 xi[A];
+    float rm2[A], vt[A];
+#pragma unroll
+    for (int u = 0; u < A; ++u) {
+        active[u] = t + u * kT < item.z;
+        ai[u] = item.y + (active[u] ? t + u * kT : 0);
+        xi[u] = a.pos[ai[u]];
+        const int ity = a.atype[ai[u]].y;
+        const float rm = __ldg(a.rmax + ity);
+        rm2[u] = __fmul_rn(rm, rm);
+        frow[u] = ity * nf;
+        vt[u] = __ldg(a.vtot + ity);
+    }
     // Per-stage FP32 partial sums (at most kForceThreads points) are folded into
     // per-thread fixed-point registers, so FP32 rounding never spans more than
-    // one stage; one set of atomics per work item.
-    long long fxa = 0, fya = 0, fza = 0;
+    // one stage; one set of atomics per atom and work item.
+    long long fxa[A], fya[A], fza[A];
+#pragma unroll
+    for (int u = 0; u < A; ++u) fxa[u] = fya[u] = fza[u] = 0;
 
     for (int p0 = 0; p0 < ch.y; p0 += kForceThreads) {
-        float qx = 0.f, qy = 0.f, qz = 0.f;  // polarisation terms, per unit -q_i vtot_i
-        float lx = 0.f, ly = 0.f, lz = 0.f;  // tabulated LJ, per unit -vtot_i
+        float qx[A], qy[A], qz[A];  // polarisation terms, per unit -q_i vtot_i
+        float lx[A], ly[A], lz[A];  // tabulated LJ, per unit -vtot_i
+#pragma unroll
+        for (int u = 0; u < A; ++u) qx[u] = qy[u] = qz[u] = lx[u] = ly[u] = lz[u] = 0.f;
         const int pn = min(kForceThreads, ch.y - p0);
         __syncthreads();
-        if (t < pn) {
-            const long long pg = (long long)ch.x + p0 + t;
-            s_p[t].q[0] = a.pts.q0[pg];
-            s_p[t].q[1] = a.pts.q1[pg];
-            s_p[t].q[2] = a.pts.q2[pg];
-            s_p[t].q[3] = a.pts.q3[pg];
-            s_p[t].q[4] = a.pts.q4[pg];
+        for (int i = t; i < pn; i += kT) {
+            const long long pg = (long long)ch.x + p0 + i;
+            s_p[i].q[0] = a.pts.q0[pg];
+            s_p[i].q[1] = a.pts.q1[pg];
+            s_p[i].q[2] = a.pts.q2[pg];
+            s_p[i].q[3] = a.pts.q3[pg];
+            s_p[i].q[4] = a.pts.q4[pg];
         }
         __syncthreads();
-#pragma unroll 2
+#pragma unroll 4
         for (int k = 0; k < pn; ++k) {
             const float4 *R = s_p[k].q;
             const float4 P = R[0];
-            const float rx = mimg(P.x - xi.x, L, h);
-            const float ry = mimg(P.y - xi.y, L, h);
-            const float rz = mimg(P.z - xi.z, L, h);
-            const float d2 = dist2f(rx, ry, rz);
-            const bool inside = d2 <= rm2;  // (:291)
-            const float ri = rsqrtf(d2);
-            const float ri2 = ri * ri;
-            const float ri3 = ri2 * ri;
-            const float ri5 = ri3 * ri2;
             const float4 E = R[1];
             const float4 K = R[2];
-            const float4 D = R[inside ? 3 : 4];
-            // multipole (:274-289) with the CDD term (:306-312) folded into D
-            const float w = fmaf(E.x, rx, fmaf(E.y, ry, E.z * rz));
-            const float dD = fmaf(D.x, rx, fmaf(D.y, ry, D.z * rz));
-            const float g = w * ri2;
-            float X = (w * g) * fmaf(K.y, g, K.x);
-            X = fmaf(3.0f, dD, X) - E.w;
-            X = fmaf(-K.w, g, X);
-            const float cR = X * ri5;
-            const float cE = fmaf(-D.w, ri2, fmaf(K.w, g, K.z) * g) * ri3;
-            qx = fmaf(cR, rx, fmaf(-cE, E.x, fmaf(-ri3, D.x, qx)));
-            qy = fmaf(cR, ry, fmaf(-cE, E.y, fmaf(-ri3, D.y, qy)));
-            qz = fmaf(cR, rz, fmaf(-cE, E.z, fmaf(-ri3, D.z, qz)));
-            if (LJ && inside) {  // tabulated mean LJ force (:291-305)
-                const float dist = __fsqrt_rn(d2);
-                const int bin = (int)__fmaf_rn(__fsub_rn(dist, f_r0), f_inv, 0.5f);
-                if (bin >= 0 && bin < nf) {
-                    const float2 tv = __ldg(a.ftab + frow + bin);
-                    const float fr = (dist - fmaf((float)bin, f_dr, f_r0)) * f_inv;
-                    const float fv = fmaf(fr, tv.y - tv.x, tv.x) * P.w * ri;
-                    lx = fmaf(fv, rx, lx);
-                    ly = fmaf(fv, ry, ly);
-                    lz = fmaf(fv, rz, lz);
+#pragma unroll
+            for (int u = 0; u < A; ++u) {
+                const float rx = mimg(P.x - xi[u].x, L, h);
+                const float ry = mimg(P.y - xi[u].y, L, h);
+                const float rz = mimg(P.z - xi[u].z, L, h);
+                const float d2 = dist2f(rx, ry, rz);
+                const bool inside = d2 <= rm2[u];  // (:291)
+                const float ri = rsqrtf(d2);
+                const float ri2 = ri * ri;
+                const float ri3 = ri2 * ri;
+                const float ri5 = ri3 * ri2;
+                const float4 D = R[inside ? 3 : 4];
+                // multipole (:274-289) with the CDD term (:306-312) folded into D
+                const float w = fmaf(E.x, rx, fmaf(E.y, ry, E.z * rz));
+                const float dD = fmaf(D.x, rx, fmaf(D.y, ry, D.z * rz));
+                const float g = w * ri2;
+                float X = (w * g) * fmaf(K.y, g, K.x);
+                X = fmaf(3.0f, dD, X) - E.w;
+                X = fmaf(-K.w, g, X);
+                const float cR = X * ri5;
+                const float cE = fmaf(-D.w, ri2, fmaf(K.w, g, K.z) * g) * ri3;
+                qx[u] = fmaf(cR, rx, fmaf(-cE, E.x, fmaf(-ri3, D.x, qx[u])));
+                qy[u] = fmaf(cR, ry, fmaf(-cE, E.y, fmaf(-ri3, D.y, qy[u])));
+                qz[u] = fmaf(cR, rz, fmaf(-cE, E.z, fmaf(-ri3, D.z, qz[u])));
+                if (LJ && inside) {  // tabulated mean LJ force (:291-305)
+                    const float dist = __fsqrt_rn(d2);
+                    const int bin = (int)__fmaf_rn(__fsub_rn(dist, f_r0), f_inv, 0.5f);
+                    if (bin >= 0 && bin < nf) {
+                        const float2 tv = __ldg(a.ftab + frow[u] + bin);
+                        const float fr = (dist - fmaf((float)bin, f_dr, f_r0)) * f_inv;
+                        const float fv = fmaf(fr, tv.y - tv.x, tv.x) * P.w * ri;
+                        lx[u] = fmaf(fv, rx, lx[u]);
+                        ly[u] = fmaf(fv, ry, ly[u]);
+                        lz[u] = fmaf(fv, rz, lz[u]);
+                    }
                 }
             }
         }
-        const float Fx = -vt * fmaf(xi.w, qx, lx);
-        const float Fy = -vt * fmaf(xi.w, qy, ly);
-        const float Fz = -vt * fmaf(xi.w, qz, lz);
-        if (active) check_force(a.status, Fx, Fy, Fz);
-        fxa += to_fix(Fx);
-        fya += to_fix(Fy);
-        fza += to_fix(Fz);
+#pragma unroll
+        for (int u = 0; u < A; ++u) {
+            const float Fx = -vt[u] * fmaf(xi[u].w, qx[u], lx[u]);
+            const float Fy = -vt[u] * fmaf(xi[u].w, qy[u], ly[u]);
+            const float Fz = -vt[u] * fmaf(xi[u].w, qz[u], lz[u]);
+            if (active[u]) check_force(a.status, Fx, Fy, Fz);
+            fxa[u] += to_fix(Fx);
+            fya[u] += to_fix(Fy);
+            fza[u] += to_fix(Fz);
+        }
     }
-    if (!active) return;
-    unsigned long long *acc = a.facc + 3 * (long long)ai;
-    atomicAdd(acc + 0, (unsigned long long)fxa);
-    atomicAdd(acc + 1, (unsigned long long)fya);
-    atomicAdd(acc + 2, (unsigned long long)fza);
+#pragma unroll
+    for (int u = 0; u < A; ++u) {
+        if (!active[u]) continue;
+        unsigned long long *acc = a.facc + 3 * (long long)ai[u];
+        atomicAdd(acc + 0, (unsigned long long)fxa[u]);
+        atomicAdd(acc + 1, (unsigned long long)fya[u]);
+        atomicAdd(acc + 2, (unsigned long long)fza[u]);
+    }
 }
 
 template <int S, bool GEN, bool RAW>
@@ -379,16 +408,24 @@ int field_blocks_per_sm(int split) {
     }
 }
 
-int force_blocks_per_sm() {
+int force_blocks_per_sm(int atoms_per_thread) {
     int n = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, force_kernel<true>, kForceThreads, 0);
+    if (atoms_per_thread == 2)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, force_kernel<true, 2>, ForceShape<2>::kThreads, 0);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, force_kernel<true, 1>, ForceShape<1>::kThreads, 0);
     return n;
 }
 
 void launch_force(const ForceArgs &a, cudaStream_t s) {
     if (a.n_items <= 0) return;
-    if (a.terms & 2) force_kernel<true><<<a.n_items, kForceThreads, 0, s>>>(a);
-    else force_kernel<false><<<a.n_items, kForceThreads, 0, s>>>(a);
+    if (a.atoms_per_thread == 2) {
+        if (a.terms & 2) force_kernel<true, 2><<<a.n_items, ForceShape<2>::kThreads, 0, s>>>(a);
+        else force_kernel<false, 2><<<a.n_items, ForceShape<2>::kThreads, 0, s>>>(a);
+    } else {
+        if (a.terms & 2) force_kernel<true, 1><<<a.n_items, ForceShape<1>::kThreads, 0, s>>>(a);
+        else force_kernel<false, 1><<<a.n_items, ForceShape<1>::kThreads, 0, s>>>(a);
+    }
 }
 
 }  // namespace isspa

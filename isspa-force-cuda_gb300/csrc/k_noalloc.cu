@@ -144,7 +144,7 @@ extern "C" int isspa_force_noalloc(const isspa_noalloc_inputs *in_p, float *forc
     }
     const int tp = field_points_per_block(S);
     const long long atiles = (in.n_atoms + 127) / 128;
-    const long long fslots = (long long)sms * std::max(1, force_blocks_per_sm());
+    const long long fslots = (long long)sms * std::max(1, force_blocks_per_sm(1));
     long long C = std::max<long long>(64, std::min<long long>(8192, (atiles * P + 2 * fslots - 1) / (2 * fslots)));
     const long long n_tiles = (P + tp - 1) / tp, n_chunks = (P + C - 1) / C, n_items = atiles * n_chunks;
 

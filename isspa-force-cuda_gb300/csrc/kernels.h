@@ -45,6 +45,7 @@ struct ForceArgs {
     int n_f;
     float f_r0, f_dr, f_inv;
     int terms;             // 1 multipole, 2 tabulated LJ, 4 CDD
+    int atoms_per_thread;  // 1 (128-thread blocks) or 2 (64-thread blocks)
     unsigned long long *facc;  // [Ntot][3]
     int *status;
 };
@@ -206,6 +207,6 @@ int nonbond_block_threads();
 // launch-shape helpers for the work-list builder
 int field_points_per_block(int split);
 int field_blocks_per_sm(int split);
-int force_blocks_per_sm();
+int force_blocks_per_sm(int atoms_per_thread);
 
 }  // namespace isspa

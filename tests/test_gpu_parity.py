@@ -177,6 +177,24 @@ def test_graph_step_equals_call_sequence(synth_medium):
     assert a.get_step() == 10
 
 
+@pytest.mark.parametrize("chunk", [128, 37])
+def test_force_kernel_atoms_per_thread_bit_identical(synth_medium, chunk):
+    """With the same point chunks, the 2-atoms-per-thread force kernel gives the
+    1-atom kernel's forces bit for bit (each atom sees the same arithmetic in
+    the same order), also with a ragged chunk and partial atom tiles."""
+    out = []
+    for apt in (1, 2):
+        eng = ig.Engine(synth_medium, force_atoms_per_thread=apt, force_chunk=chunk)
+        assert eng.shapes()["force_atoms_per_thread"] == apt
+        eng.zero_forces()
+        eng.isspa_force()
+        out.append(eng.forces())
+        eng.step(3)
+        out.append(eng.positions())
+    assert np.array_equal(out[0], out[2])
+    assert np.array_equal(out[1], out[3])
+
+
 def test_point_injection(adi2_100):
     s = adi2_100
     o = O.Oracle(s)
