@@ -306,8 +306,22 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def _cu_profiler(on: bool):
+    """cuProfilerStart/Stop of the driver API: with `ncu --profile-from-start
+    off` only the launches in between are profiled."""
+    import ctypes as C
+
+    drv = C.CDLL("libcuda.so.1")
+    rc = drv.cuProfilerStart() if on else drv.cuProfilerStop()
+    if rc != 0:
+        raise RuntimeError(f"cuProfiler{'Start' if on else 'Stop'} returned {rc}")
+
+
 def run_profile_case(args):
-    """Untimed graph steps of a workload, for ncu launch lists and captures."""
+    """Graph steps of a workload for ncu launch lists and captures: the same
+    engine and autotuned launch shapes as the benchmark, then `profile_steps`
+    steps inside a cuProfilerStart/Stop range (run ncu with
+    --profile-from-start off to skip the autotuner's trial launches)."""
     import build as engine_build
     import isspa_gb300 as ig
 
@@ -318,10 +332,15 @@ def run_profile_case(args):
         eng = ig.Engine(ig.synth.config_precision(seed=3))
     else:
         eng = ig.Engine(ig.synth.config_plain(seed=2))
+    shapes = eng.shapes() if args.no_autotune else eng.autotune()
+    eng.step(2)
+    eng.synchronize()
+    _cu_profiler(True)
     eng.step(args.profile_steps)
     eng.synchronize()
+    _cu_profiler(False)
     print(json.dumps({"profile_case": args.workload, "steps": args.profile_steps, "atoms": eng.n_atoms,
-                      "points": eng.n_points}))
+                      "points": eng.n_points, "launch_shapes": shapes}))
 
 
 def main():
