@@ -3,11 +3,14 @@
 Each translation unit is compiled by nvcc in parallel and linked into one
 shared library next to this file; nothing is installed.  Host code carries no
 architecture-specific flags so the same sources build on x86-64 and aarch64.
+Objects are kept per host architecture (_build/<machine>/) and recompiled only
+when their source or a header changed.
 """
 from __future__ import annotations
 
 import concurrent.futures as cf
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -16,7 +19,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
-BUILD = os.path.join(HERE, "_build")
+BUILD = os.path.join(HERE, "_build", platform.machine() or "host")
+STAMP = os.path.join(BUILD, "linked")  # the library beside this file was linked from these objects
 LIB = os.path.join(HERE, "libisspa_gb300.so")
 EXE = os.path.join(HERE, "total_force_gb300")
 
@@ -62,16 +66,24 @@ def _stale(target: str, deps) -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
+def _obj(src: str) -> str:
+    return os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
+
+
 def build(verbose: bool = False, force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers.append(os.path.join(INCLUDE, "isspa_gb300.h"))
-    srcs = [os.path.join(CSRC, s) for s in SOURCES] + [os.path.join(CSRC, "main_total_force.cpp")]
-    if not force and not _stale(LIB, srcs + headers) and not _stale(EXE, srcs + headers):
+    units = SOURCES + ["main_total_force.cpp"]
+    srcs = [os.path.join(CSRC, s) for s in units]
+    fresh = os.path.exists(STAMP) and not _stale(STAMP, srcs + headers)
+    if not force and fresh and not _stale(LIB, [STAMP]) and not _stale(EXE, [STAMP]):
         return LIB
-    with cf.ThreadPoolExecutor(max_workers=len(SOURCES) + 1) as ex:
-        futs = [ex.submit(_compile, s, verbose) for s in SOURCES + ["main_total_force.cpp"]]
-        objs = [f.result() for f in futs]
+    todo = [s for s in units if force or _stale(_obj(s), [os.path.join(CSRC, s)] + headers)]
+    with cf.ThreadPoolExecutor(max_workers=max(1, len(todo))) as ex:
+        for f in [ex.submit(_compile, s, verbose) for s in todo]:
+            f.result()
+    objs = [_obj(s) for s in units]
     lib_objs, main_obj = objs[:-1], objs[-1]
     tmp = LIB + ".tmp"
     r = subprocess.run([nvcc()] + ARCH + ["-shared", "-o", tmp] + lib_objs, capture_output=True, text=True)
@@ -82,6 +94,8 @@ def build(verbose: bool = False, force: bool = False) -> str:
                         "-Xlinker", "-rpath,$ORIGIN"], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link of the drop-in executable failed:\n{r.stdout}\n{r.stderr}")
+    with open(STAMP, "w") as f:
+        f.write(platform.machine() + "\n")
     return LIB
 
 
