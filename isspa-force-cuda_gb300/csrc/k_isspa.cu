@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(FieldShape<S>::kThreads) field_kernel(FieldArg
             s_row[threadIdx.x] = a.atype[j].y * nb;
         }
         __syncthreads();
-#pragma unroll 2
+#pragma unroll 4
         for (int k = sp; k < jn; k += S) {
             const float4 xj = s_atom[k];
             const float rx = mimg(px - xj.x, L, h);
