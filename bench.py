@@ -6,7 +6,7 @@ atoms, nMC = 50, 60 A box, all-pairs FP32 nonbond + IS-SPA, Andersen at
 One step = one full MD step: bonded, IS-SPA field + force, nonbond,
 leapfrog (graph-replayed).
 
-  python bench.py [--steps K] [--warmup W] [--impl gb300|reference] [--no-batched]
+  python bench.py [--steps K] [--warmup W] [--impl gb300|reference] [--no-batched] [--no-extra]
 
 The gb300 arm prints one JSON line with device-timed throughput, the end-to-end
 figure through the C ABI with host buffers, the roofline of the dominant
@@ -261,6 +261,9 @@ def run_gb300(args):
     line["clocks"] = clocks
     if not args.no_batched:
         line["batched"] = run_batched(ig, args, value)
+    if not args.no_extra:
+        line["precision"] = run_precision(ig, args, peak_fp32)
+        line["adjoint"] = run_adjoint(ig)
     print(json.dumps(line))
 
 
@@ -289,6 +292,53 @@ def run_batched(ig, args, plain_value):
             "plain_per_window_value": round(plain, 1), "speedup_vs_plain": round(batched / plain, 2),
             "launch_shapes": shapes,
             "kernel_ms_per_step": {k: round(v[0] / max(v[1], 1), 4) for k, v in kern.items()}}
+
+
+def run_precision(ig, args, peak_fp32):
+    """16 384-atom precision workload (256 x 64-atom chains, nMC 100, 1.64 M MC
+    points): device-timed graph steps and the force kernel's FP32 rate."""
+    s = ig.synth.config_precision(seed=3)
+    N, P = s.n_atoms, s.n_atoms * s.n_mc
+    eng = ig.Engine(s)
+    shapes = eng.shapes() if args.no_autotune else eng.autotune(reps=1)
+    eng.step(2)
+    steps = 5
+    ms, kern = eng.time_steps_detailed(steps, L2_FLUSH)
+    status = eng.device_status()
+    eng.close()
+    avg = {k: v[0] / v[1] for k, v in kern.items() if v[1] > 0}
+    force_tf = FLOP_FORCE_PAIR * N * P / (avg["force"] * 1e-3) / 1e12
+    field_tf = (FLOP_FIELD_PAIR * N * P + FLOP_POINT * P) / (avg["field"] * 1e-3) / 1e12
+    return {"workload": "256 x 64-atom chains (16384 atoms), nMC=100 (1.64 M points), 120 A box, charges +-0.8 e",
+            "steps": steps, "value": round(N * steps / (ms * 1e-3), 1), "unit": UNIT,
+            "ms_per_step": round(ms / steps, 3),
+            "ns_per_day": round(ns_per_day(steps / (ms * 1e-3)), 2),
+            "kernel_ms_per_launch": {k: round(v, 3) for k, v in avg.items()},
+            "force_kernel_tflops": round(force_tf, 2), "force_kernel_frac": round(force_tf / peak_fp32, 4),
+            "field_kernel_tflops": round(field_tf, 2), "field_kernel_frac": round(field_tf / peak_fp32, 4),
+            "launch_shapes": shapes, "device_status": status,
+            "force_error": "sampled against the FP64 oracle in tests/test_gpu_precision.py"}
+
+
+def run_adjoint(ig):
+    """Differentiation workload: 16 umbrella windows of 550 atoms (nMC 50), the
+    adjoint of the window mean forces for one frame (MC points regenerated),
+    wall time per call including its host-side set-up."""
+    wins = ig.synth.config_adjoint()
+    eng = ig.Engine(wins)
+    eng.step(3)
+    eng.adjoint_mean_force([3])
+    reps = 5
+    t0 = time.perf_counter()
+    for k in range(reps):
+        eng.adjoint_mean_force([4 + k])
+    dt = (time.perf_counter() - t0) / reps
+    status = eng.device_status()
+    eng.close()
+    return {"workload": "16 windows x 550 atoms (25 x 22-atom chains), nMC=50, 50 A box, r0 5..12 A",
+            "ms_per_frame": round(dt * 1e3, 3), "frames_per_s": round(1.0 / dt, 1), "timing": "host wall clock",
+            "device_status": status,
+            "accuracy": "dJ/dtheta within 4.4e-7 of FP64 central differences (tests/test_gpu_adjoint.py)"}
 
 
 def run_reference(args):
@@ -360,6 +410,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the precision-workload and adjoint sections")
     ap.add_argument("--no-autotune", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)

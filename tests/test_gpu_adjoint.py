@@ -99,3 +99,28 @@ def test_adjoint_repeat_calls_agree(setup):
     b = eng.adjoint_mean_force(steps, frames)
     for x, y in zip(a, b):
         assert np.abs(x - y).max() <= 1e-12 * max(np.abs(x).max(), 1e-300)
+
+
+@pytest.mark.slow
+def test_adjoint_full_differentiation_workload():
+    """The differentiation workload at full size (16 windows of 550 atoms,
+    nMC 50, r0 5..12 A): J and dJ/dtables of the first and last windows against
+    the oracle's naive FP64 adjoint for one frame (1e-5 relative)."""
+    wins = synth.config_adjoint()
+    eng = ig.Engine(wins)
+    eng.step(20)
+    pos = eng.positions()
+    J, df, dg, dA, dB = eng.adjoint_mean_force([20])
+    n = wins[0].n_atoms
+    for w in (0, len(wins) - 1):
+        s = wins[w].copy()
+        s.pos = pos[w * n:(w + 1) * n]
+        o = O.Oracle(s)
+        pts = o.mc_points(seed=s.seed, step=20, window=w)
+        _, a, b, c, d = o.adjoint(pts)
+        Jo = o.mean_force(pts)  # J also carries the bonded forces
+        print(f"window {w}: J gpu {J[w]:.6f} oracle {Jo:.6f}")
+        assert abs(J[w] - Jo) <= 1e-5 * max(abs(Jo), 1.0)
+        for got, ref in zip((df[w], dg[w], dA[w], dB[w]), (a, b, c, d)):
+            assert np.abs(got - ref).max() <= 1e-5 * max(np.abs(ref).max(), 1e-300)
+    assert eng.device_status() == 0
