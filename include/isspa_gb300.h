@@ -169,7 +169,7 @@ int isspa_engine_info(const isspa_engine *e, int *n_windows, int *n_atoms_total,
 int isspa_engine_shapes(const isspa_engine *e, int shape[ISSPA_SHAPE_COUNT]);
 /* Autotuner: times every field-pass atom split and, for 1 and 2 receiving
  * atoms per force thread, a set of force-pass chunk lengths (those filling
- * 1..6 whole waves of resident blocks, and powers of two) on this engine's own
+ * 1..12 whole waves of resident blocks, and powers of two) on this engine's own
  * workload with CUDA events (reps launches each), keeps the fastest of each
  * and reports the result as isspa_engine_shapes does.  Clears the force
  * accumulator; invalidates captured graphs. */

@@ -179,7 +179,7 @@ struct isspa_engine {
         const long long slots = (long long)n_sms * std::max(1, force_blocks_per_sm(force_apt));
         double best = -1.0;
         int C = 64;
-        for (long long c = 8192; c >= 64; --c) {  // longest chunk (fewest atomics) at equal efficiency
+        for (long long c = 8192; c >= 32; --c) {  // longest chunk (fewest atomics) at equal efficiency
             const long long n = force_items_for(c);
             const double e = n < slots ? 0.5 * (double)n / (double)slots : wave_eff(n, slots);
             if (e > best + 0.005) {
@@ -212,8 +212,10 @@ struct isspa_engine {
             for (long long p = 0; p < P; p += C)
                 chunks.push_back(make_int2((int)(d.point_off + p), (int)std::min<long long>(C, P - p)));
             const int nc = (int)chunks.size() - c0;
-            for (int a = 0; a < d.n_atoms; a += 128)
-                for (int c = 0; c < nc; ++c)
+            // chunk-major: blocks that run together read the same point records
+            // and add into different atom tiles' accumulators
+            for (int c = 0; c < nc; ++c)
+                for (int a = 0; a < d.n_atoms; a += 128)
                     items.push_back(make_int4(w, d.atom_off + a, std::min(128, d.n_atoms - a), c0 + c));
         }
         release(force_items);
@@ -1164,7 +1166,7 @@ int isspa_autotune(isspa_engine *e, int reps, int shape[ISSPA_SHAPE_COUNT]) {
         e->set_field_split(bestS);
         launch_field(e->field_args(), bestS, false, e->stream);
         // force pass: for 1 and 2 atoms per thread, the chunk lengths that fill
-        // 1..6 whole waves of that kernel's resident blocks, and powers of two
+        // 1..12 whole waves of that kernel's resident blocks, and powers of two
         long long maxP = 0;
         for (const WinDev &d : e->win_h) maxP = std::max(maxP, (long long)d.n_atoms * e->n_mc);
         best = 1e30f;
@@ -1173,8 +1175,8 @@ int isspa_autotune(isspa_engine *e, int reps, int shape[ISSPA_SHAPE_COUNT]) {
             e->force_apt = apt;
             const long long slots = (long long)e->n_sms * std::max(1, force_blocks_per_sm(apt));
             std::vector<int> cands = {e->default_force_chunk()};
-            for (int k = 1; k <= 6; ++k) {
-                long long lo = 64, hi = std::max<long long>(64, std::min<long long>(8192, maxP));
+            for (int k = 1; k <= 12; ++k) {
+                long long lo = 32, hi = std::max<long long>(32, std::min<long long>(8192, maxP));
                 while (lo < hi) {  // smallest C with items <= k * slots
                     const long long mid = (lo + hi) / 2;
                     if (e->force_items_for(mid) <= k * slots) hi = mid;
