@@ -13,9 +13,11 @@
 //          The per-point prologue of the reference's force kernel (|E|, unit
 //          field, Langevin averages, 1/n; :253-273) is computed here once per
 //          point instead of once per (atom, point) pair.
-//  force:  one thread per receiving atom; MC points are streamed through shared
-//          memory in chunks (broadcast reads); per-thread FP32 partial sums are
-//          flushed once per chunk into int64 fixed-point accumulators, so the
+//  force:  one thread per receiving atom (or two); work items are (window,
+//          128-atom tile, point chunk), and each item streams its points
+//          through shared memory in stages of 128 (broadcast reads); per-thread
+//          FP32 partial sums are flushed once per stage into int64 fixed-point
+//          registers and once per item into the atom's accumulator, so the
 //          final force is independent of scheduling order.
 #include <cuda_runtime.h>
 
