@@ -142,6 +142,12 @@ int isspa_read_run_config(const char *path, isspa_run_config *out);
 int isspa_system_load(const isspa_run_config *cfg, const char *base_dir, isspa_host_system **out);
 int isspa_read_prmtop(const char *path, float eps, isspa_host_system **out);
 int isspa_read_isspatop(isspa_host_system *sys, const char *path);
+/* Writes the IS-SPA sections of desc (types, rmax, density / field / force
+ * tables with their radial grids) as an .isspatop file that
+ * isspa_read_isspatop reads back exactly; replaces the table writer of
+ * scripts/isspa_prmtop/write_isspa_prmtop.py:202-273, with ISSPA_FORCES in the
+ * linear form the reader (isspa_class.cpp:155-170) uses. */
+int isspa_write_isspatop(const isspa_system_desc *desc, const char *path, const char *title);
 int isspa_read_rst7(isspa_host_system *sys, const char *path, int velocities);
 int isspa_read_us_config(isspa_host_system *sys, const char *path, char *cv_file_out, size_t cv_len);
 /* Points desc at the host system's arrays (valid until isspa_system_free). */

@@ -618,6 +618,44 @@ int isspa_system_describe(const isspa_host_system *s, isspa_system_desc *d) {
 
 void isspa_system_free(isspa_host_system *s) { delete s; }
 
+// The sections isspa_read_isspatop reads, in the layout of the reference's
+// .isspatop files (isspa_class.cpp:45-178; written there by
+// scripts/isspa_prmtop/write_isspa_prmtop.py:202-273).  ISSPA_FORCES is written
+// as the linear values the CUDA reader uses (isspa_class.cpp:155-170), not the
+// logarithm that script stores.  Radii are r0 + i dr; values carry 9
+// significant digits, so every float table entry reads back exactly.
+int isspa_write_isspatop(const isspa_system_desc *d, const char *path, const char *title) {
+    if (!d || !path || d->n_atoms <= 0 || d->n_isspa_types <= 0 || !d->isspa_type || !d->rmax || !d->g_table ||
+        !d->e_table || !d->f_table || d->n_g < 2 || d->n_e < 2 || d->n_f < 2)
+        return ISSPA_ERR_ARG;
+    const int N = d->n_atoms, nt = d->n_isspa_types;
+    for (int i = 0; i < N; ++i)
+        if (d->isspa_type[i] < 0 || d->isspa_type[i] >= nt) return ISSPA_ERR_ARG;
+    std::FILE *f = std::fopen(path, "w");
+    if (!f) return ISSPA_ERR_IO;
+    std::fprintf(f, "%%VERSION \n%%FLAG TITLE\n%%FORMAT(20a4)\n%.80s\n", title ? title : "");
+    std::fprintf(f, "%%FLAG POINTERS\n%%FORMAT(10I8)\n%8d%8d%8d%8d%8d\n", N, nt, d->n_g, d->n_e, d->n_f);
+    std::fprintf(f, "%%FLAG ISSPA_TYPE_INDEX\n%%FORMAT(10I8)\n");
+    for (int i = 0; i < N; ++i)
+        std::fprintf(f, "%8d%s", d->isspa_type[i] + 1, (i % 10 == 9 || i == N - 1) ? "\n" : "");
+    std::fprintf(f, "%%FLAG ISSPA_RMAX\n%%FORMAT(5E16.8)\n");
+    for (int t = 0; t < nt; ++t)
+        std::fprintf(f, "%16.8e%s", (double)d->rmax[t], (t % 5 == 4 || t == nt - 1) ? "\n" : "");
+    auto table = [&](const char *flag, int rows, const float *tab, float r0, float dr) {
+        std::fprintf(f, "%%FLAG %s\n%%FORMAT(%dE16.8)\n", flag, nt + 1);
+        for (int i = 0; i < rows; ++i) {
+            std::fprintf(f, "%16.8e", (double)r0 + (double)i * (double)dr);
+            for (int t = 0; t < nt; ++t) std::fprintf(f, "%16.8e", (double)tab[(size_t)t * rows + i]);
+            std::fprintf(f, "\n");
+        }
+    };
+    table("ISSPA_DENSITIES", d->n_g, d->g_table, d->g_r0, d->g_dr);
+    table("ISSPA_EFIELD", d->n_e, d->e_table, d->e_r0, d->e_dr);
+    table("ISSPA_FORCES", d->n_f, d->f_table, d->f_r0, d->f_dr);
+    const bool ok = std::ferror(f) == 0;
+    return (std::fclose(f) == 0 && ok) ? ISSPA_OK : ISSPA_ERR_IO;
+}
+
 }  // extern "C"
 
 namespace isspa {

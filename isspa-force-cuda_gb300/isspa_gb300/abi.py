@@ -93,6 +93,7 @@ SIGNATURES = [
     ("isspa_system_load", C.c_int, [C.POINTER(RunConfig), C.c_char_p, C.POINTER(_P)]),
     ("isspa_read_prmtop", C.c_int, [C.c_char_p, C.c_float, C.POINTER(_P)]),
     ("isspa_read_isspatop", C.c_int, [_P, C.c_char_p]),
+    ("isspa_write_isspatop", C.c_int, [_P, C.c_char_p, C.c_char_p]),
     ("isspa_read_rst7", C.c_int, [_P, C.c_char_p, C.c_int]),
     ("isspa_read_us_config", C.c_int, [_P, C.c_char_p, C.c_char_p, C.c_size_t]),
     ("isspa_system_describe", C.c_int, [_P, C.POINTER(SystemDesc)]),

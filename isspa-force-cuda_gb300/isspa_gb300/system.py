@@ -194,6 +194,12 @@ class System:
             us_k=d.us_k, us_x0=d.us_x0,
         )
 
+    def write_isspatop(self, path: str, title: str = "") -> None:
+        """Write this system's IS-SPA types, rmax and tables as an .isspatop file
+        (the inverse of the reader used by from_config)."""
+        d, keep = self.to_desc()
+        abi.check(abi.lib().isspa_write_isspatop(C.byref(d), path.encode(), title.encode()), path)
+
     @staticmethod
     def from_config(path: str) -> "System":
         """Read a reference config file and everything it names (total_force_cuda.cpp:57-99)."""
