@@ -74,3 +74,19 @@ def test_dropin_outputs(rundir):
     assert np.allclose(pos[0], s.pos[:, :3], atol=1.5e-6)
     com, cvv = eng.us_com()
     assert abs(float(cv[0].split()[1]) - cvv[0]) < 1e-3
+
+
+def test_dropin_long_run_autotunes(rundir):
+    """A run of 1000 steps or more times the launch-shape candidates first and
+    reports the choice; the run completes with its CV file intact."""
+    cfg = (rundir / "config.txt").read_text()
+    (rundir / "config.txt").write_text(cfg.replace("nSteps = 25", "nSteps = 2000").replace("deltaWrite = 10",
+                                                                                              "deltaWrite = 500"))
+    r = subprocess.run([EXE, "config.txt"], cwd=rundir, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert "launch shapes: field split" in r.stdout
+    cv = [ln for ln in (rundir / "ADI2.equil.window.10.0.dat").read_text().splitlines() if ln.strip()]
+    assert [int(c.split()[0]) for c in cv] == [0, 500, 1000, 1500]
+    pos = read_xyz_frames(rundir / "ADI2.positions.xyz", 3)
+    assert len(pos) == 4
+    assert all(np.all(np.isfinite(p)) for p in pos)
