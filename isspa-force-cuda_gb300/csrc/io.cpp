@@ -685,22 +685,35 @@ int host_system_from_desc(const isspa_system_desc &d, isspa_host_system &s) {
     else s.n_excl_cum.assign(N, 0);
     if (d.excl_len > 0 && d.excl_list) cp(d.excl_list, d.excl_len, s.excl_list);
     else s.excl_list.clear();
+    // parameter tables whenever types are declared (a system may declare
+    // types and have no terms of that kind); terms only when present
+    if (d.n_bond_types < 0 || d.n_angle_types < 0 || d.n_dih_types < 0 || d.n_bonds < 0 || d.n_angles < 0 ||
+        d.n_dihs < 0)
+        return ISSPA_ERR_ARG;
+    if ((d.n_bond_types > 0 && !d.bond_params) || (d.n_angle_types > 0 && !d.angle_params) ||
+        (d.n_dih_types > 0 && (!d.dih_params || !d.scaled14)))
+        return ISSPA_ERR_ARG;
     s.n_bond_types = d.n_bond_types;
+    if (d.n_bond_types > 0) cp(d.bond_params, 2 * (size_t)d.n_bond_types, s.bond_params);
     if (d.n_bonds > 0) {
+        if (!d.bond_atoms) return ISSPA_ERR_ARG;
         cp(d.bond_atoms, 3 * (size_t)d.n_bonds, s.bond_atoms);
-        cp(d.bond_params, 2 * (size_t)d.n_bond_types, s.bond_params);
     }
     s.n_angle_types = d.n_angle_types;
+    if (d.n_angle_types > 0) cp(d.angle_params, 2 * (size_t)d.n_angle_types, s.angle_params);
     if (d.n_angles > 0) {
+        if (!d.angle_atoms) return ISSPA_ERR_ARG;
         cp(d.angle_atoms, 4 * (size_t)d.n_angles, s.angle_atoms);
-        cp(d.angle_params, 2 * (size_t)d.n_angle_types, s.angle_params);
     }
     s.n_dih_types = d.n_dih_types;
-    if (d.n_dihs > 0) {
-        cp(d.dih_atoms, 4 * (size_t)d.n_dihs, s.dih_atoms);
-        cp(d.dih_types, d.n_dihs, s.dih_types);
+    if (d.n_dih_types > 0) {
         cp(d.dih_params, 4 * (size_t)d.n_dih_types, s.dih_params);
         cp(d.scaled14, 2 * (size_t)d.n_dih_types, s.scaled14);
+    }
+    if (d.n_dihs > 0) {
+        if (!d.dih_atoms || !d.dih_types) return ISSPA_ERR_ARG;
+        cp(d.dih_atoms, 4 * (size_t)d.n_dihs, s.dih_atoms);
+        cp(d.dih_types, d.n_dihs, s.dih_types);
     }
     s.have_isspa = true;
     cp(d.isspa_type, N, s.isspa_type);
