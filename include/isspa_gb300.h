@@ -108,7 +108,8 @@ typedef struct isspa_engine_options {
     int use_graph;       /* isspa_step captures the step in a CUDA graph (default 1) */
     int field_split;     /* atom-loop split per MC point in the field kernel; 0 => auto */
     int force_chunk;     /* MC points per force-kernel work item; 0 => auto */
-    size_t mem_cap;      /* device bytes the engine may allocate; 0 => unlimited */
+    size_t mem_cap;      /* device bytes the engine may hold, including the temporary
+                            buffers of the list queries; 0 => unlimited */
     int force_atoms_per_thread;  /* receiving atoms per IS-SPA force thread, 1 or 2; 0 => 1 */
 } isspa_engine_options;
 

@@ -1494,6 +1494,9 @@ int isspa_neighbor_list(isspa_engine *e, float rnn, int max_per_atom, int *rows,
     if (rc) return rc;
     const WinDev &d = e->win_h[0];
     int *d_rows = nullptr, *d_counts = nullptr;
+    // temporary buffers, freed on return, counted against the engine's cap
+    const size_t tmp = sizeof(int) * ((size_t)d.n_atoms * max_per_atom + d.n_atoms);
+    if (e->opt.mem_cap && e->allocated + tmp > e->opt.mem_cap) return ISSPA_ERR_NOMEM;
     rc = run_guarded([&] {
         ck(cudaMalloc(&d_rows, sizeof(int) * (size_t)d.n_atoms * max_per_atom));
         ck(cudaMalloc(&d_counts, sizeof(int) * d.n_atoms));
@@ -1527,6 +1530,7 @@ int isspa_cell_list(isspa_engine *e, float rc_len, const int ncell[3], int *cell
     if (rc) return rc;
     const WinDev &d = e->win_h[0];
     int *d_cell = nullptr;
+    if (e->opt.mem_cap && e->allocated + sizeof(int) * (size_t)d.n_atoms > e->opt.mem_cap) return ISSPA_ERR_NOMEM;
     rc = run_guarded([&] {
         ck(cudaMalloc(&d_cell, sizeof(int) * d.n_atoms));
         launch_cell_index(e->pos, d.atom_off, d.n_atoms, rc_len, make_int3(ncell[0], ncell[1], ncell[2]), d_cell,
