@@ -175,7 +175,11 @@ def run_gb300(args):
     eng.step(warm_steps)
     eng.synchronize()
     with ClockSampler(0) as clk:
-        total_ms, kern = eng.time_steps_detailed(args.steps, L2_FLUSH)
+        # the step as it runs (one single-step graph per timed interval), then
+        # the same step captured with an event pair around every kernel for the
+        # per-kernel durations (those event nodes lengthen the step itself)
+        total_ms = eng.time_steps(args.steps, L2_FLUSH)
+        instr_ms, kern = eng.time_steps_detailed(args.steps, L2_FLUSH)
     eng.synchronize()
     status = eng.device_status()
     ms_step = total_ms / args.steps
@@ -242,6 +246,9 @@ def run_gb300(args):
                                "all-pairs nonbond + IS-SPA, leapfrog/Andersen 298 K, dt 2 fs",
                    "n_atoms": N, "n_mc": M, "mc_points": P, "box_A": 60.0,
                    "l2": "256 MB written between timed steps (outside the timed intervals)",
+                   "timing": "value: K single-step graph replays, CUDA events around each; kernel durations: "
+                             "K more replays of the step captured with events around every kernel",
+                   "instrumented_ms_per_step": round(instr_ms / args.steps, 5),
                    "warmup_extra_steps": warm_steps,
                    "launch_shapes": shapes, "graph": True},
         "e2e": {"value": round(e2e, 1), "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes,
@@ -275,15 +282,15 @@ def run_batched(ig, args, plain_value):
     nat = sum(w.n_atoms for w in wins)
     steps = max(3, args.steps // 10)
     eng.step(3)
-    ms, kern = eng.time_steps_detailed(steps, L2_FLUSH)
+    ms = eng.time_steps(steps, L2_FLUSH)
+    _, kern = eng.time_steps_detailed(steps, L2_FLUSH)
     batched = nat * steps / (ms * 1e-3)
     # plain path: each window alone in its own engine, one after another
     plain_ms = 0.0
     for w in wins:
         e1 = ig.Engine(w)
-        e1.step(2)
-        t, _ = e1.time_steps_detailed(2, 0)
-        plain_ms += t / 2
+        e1.step(3)
+        plain_ms += e1.time_steps(10, 0) / 10
         e1.close()
     plain = nat / (plain_ms * 1e-3)
     eng.close()
@@ -303,7 +310,8 @@ def run_precision(ig, args, peak_fp32):
     shapes = eng.shapes() if args.no_autotune else eng.autotune(reps=1)
     eng.step(2)
     steps = 5
-    ms, kern = eng.time_steps_detailed(steps, L2_FLUSH)
+    ms = eng.time_steps(steps, L2_FLUSH)
+    _, kern = eng.time_steps_detailed(steps, L2_FLUSH)
     status = eng.device_status()
     eng.close()
     avg = {k: v[0] / v[1] for k, v in kern.items() if v[1] > 0}
