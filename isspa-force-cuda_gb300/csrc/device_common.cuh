@@ -62,6 +62,16 @@ struct PointsDev {
 __device__ __forceinline__ float mimg(float r, float L, float h) {
     return fabsf(r) > h ? r - copysignf(L, r) : r;
 }
+// Distance that picks a density-table bin in the field pass: r^2 times the
+// reciprocal square root the caller already holds (within a few ulp of the
+// correctly rounded root, as the reference's fast-math sqrtf).  The density
+// table is interpolated between bin and bin + 1 with the bin truncated
+// (isspa_force_cuda.cu:157-167), which is continuous across bin edges, so a bin
+// picked one rounding step off moves the result by rounding only.  The
+// mean-force table rounds to the nearest bin and interpolates from there
+// (:292-301), which jumps at half-bin edges: its distance stays the correctly
+// rounded root, the bin the oracle picks (so does the adjoint's).
+__device__ __forceinline__ float density_table_dist(float d2, float ri) { return __fmul_rn(d2, ri); }
 // Squared distance with a fixed operation sequence (no contraction freedom).
 __device__ __forceinline__ float dist2f(float x, float y, float z) {
     return __fmaf_rn(z, z, __fmaf_rn(y, y, __fmul_rn(x, x)));

@@ -121,6 +121,9 @@ __global__ void __launch_bounds__(FieldShape<S>::kThreads) field_kernel(FieldArg
     float ex = 0.f, ey = 0.f, ez = 0.f, fx = 0.f, fy = 0.f, fz = 0.f;
     const float g_r0 = a.g_r0, g_dr = a.g_dr, g_inv = a.g_inv;
     const float e_r0 = a.e_r0, e_dr = a.e_dr, e_inv = a.e_inv;
+    // the field table shares the density bin (:170-174): interpolation across
+    // that bin's edges is continuous only when both tables use one radial grid
+    const bool one_grid = g_r0 == e_r0 && g_dr == e_dr;
     const int nb = a.n_gbins;
 
     for (int j0 = 0; j0 < W.n_atoms; j0 += kT) {
@@ -150,7 +153,7 @@ __global__ void __launch_bounds__(FieldShape<S>::kThreads) field_kernel(FieldArg
                 ex = fmaf(-c, rx, ex);
                 ey = fmaf(-c, ry, ey);
                 ez = fmaf(-c, rz, ez);
-                const float dist = __fsqrt_rn(d2);
+                const float dist = one_grid ? density_table_dist(d2, ri) : __fsqrt_rn(d2);
                 const int bin = (int)__fmul_rn(__fsub_rn(dist, g_r0), g_inv);
                 if (bin < 0) {
                     w = 0.0f;

@@ -1,7 +1,9 @@
 """GPU parity: every kernel of the step against the CPU oracle, through the C ABI.
 
 Tolerances (FP32 kernels vs the FP64-valued oracle, identical geometric
-decisions by construction):
+decisions by construction, except that the field pass may pick a density-table
+bin one off at a bin edge, where its interpolation is continuous, when the
+density and field tables share one radial grid):
   * MC points, in-range counts: bit-identical;
   * per-point density product, mean field: normwise relative 2e-5;
   * per-atom forces of each term: normwise relative (max |dF| / max |F|) 2e-5,
@@ -63,9 +65,15 @@ def test_mc_points_bit_identical(adi2_100):
     assert not np.array_equal(xyz17, xyz)
 
 
-@pytest.mark.parametrize("which", ["adi2", "medium"])
+@pytest.mark.parametrize("which", ["adi2", "medium", "medium-two-grids"])
 def test_field_matches_oracle(which, adi2_100, synth_medium):
     s = adi2_100 if which == "adi2" else synth_medium
+    if which == "medium-two-grids":
+        # field table on its own radial grid: its interpolation jumps at the
+        # density bin's edges, so the bin must be the oracle's exactly
+        s = s.copy()
+        s.e_r0 = float(np.float32(s.e_r0 + 0.03))
+        s.e_dr = float(np.float32(s.e_dr * 1.1))
     eng = ig.Engine(s)
     xyz, w, n, E, E0 = eng.point_fields()
     o = O.Oracle(s)
