@@ -451,7 +451,8 @@ struct isspa_engine {
         }
         ck(cudaStreamEndCapture(stream, &g));
         cudaGraphExec_t ex = nullptr;
-        cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
+        // kernel nodes keep the priority of the stream they were captured on
+        cudaError_t e = cudaGraphInstantiate(&ex, g, cudaGraphInstantiateFlagUseNodePriority);
         cudaGraphDestroy(g);
         ck(e);
         return ex;
@@ -868,7 +869,12 @@ int isspa_engine_create(const isspa_system_desc *windows, int n_windows, const i
     }
     int rc = run_guarded([&] {
         ck(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
-        ck(cudaStreamCreateWithFlags(&e->side, cudaStreamNonBlocking));
+        // the second branch (bonded, umbrella, nonbond: a few hundred blocks)
+        // at the highest priority, so its blocks are dispatched ahead of the
+        // field and force grids' queued blocks instead of after them
+        int prio_low = 0, prio_high = 0;
+        ck(cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high));
+        ck(cudaStreamCreateWithPriority(&e->side, cudaStreamNonBlocking, prio_high));
         for (cudaEvent_t *ev : {&e->ev_fork, &e->ev_join})
             ck(cudaEventCreateWithFlags(ev, cudaEventDisableTiming));
         ck(cudaEventCreate(&e->ev_a));
