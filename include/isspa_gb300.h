@@ -211,7 +211,11 @@ enum { ISSPA_K_FIELD = 0, ISSPA_K_FORCE, ISSPA_K_NONBOND, ISSPA_K_BONDED, ISSPA_
        ISSPA_K_LEAPFROG, ISSPA_K_COUNT };
 int isspa_time_steps_detailed(isspa_engine *e, int nsteps, size_t flush_bytes, double *ms_total,
                               double *ms_kernels, int *launches);
-/* Page-locked host buffers for host<->device transfers (cudaMallocHost). */
+/* Page-locked host buffers, mapped into the device address space
+ * (cudaHostAlloc, portable and mapped).  The library keeps a registry of the
+ * live ones: isspa_step_host reads and writes buffers inside them from the GPU
+ * directly.  Release them with isspa_host_free only (never cudaFreeHost), so
+ * that the registry never holds a freed range. */
 int isspa_host_alloc(size_t bytes, void **out);
 void isspa_host_free(void *p);
 int isspa_synchronize(isspa_engine *e);
@@ -232,7 +236,11 @@ int isspa_get_step(isspa_engine *e, uint32_t *step);
 int isspa_get_us_com(isspa_engine *e, double *com, double *cv);
 
 /* One MD step with host buffers: upload pos/vel, run one full step, download
- * pos/vel/force.  This is the call a host-side driver makes per step. */
+ * pos/vel/force (float [n_atoms_total][4] each; any may be NULL).  This is
+ * the call a host-side driver makes per step.  When every non-NULL buffer is a
+ * 16-byte aligned range inside isspa_host_alloc memory, two small kernels move
+ * the state over the host link around the step; otherwise one copy per
+ * buffer.  Same results either way. */
 int isspa_step_host(isspa_engine *e, const float *pos_in, const float *vel_in, float *pos_out,
                     float *vel_out, float *force_out);
 

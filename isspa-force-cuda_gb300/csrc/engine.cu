@@ -12,9 +12,13 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdint>
 #include <cstring>
+#include <map>
 #include <memory>
+#include <mutex>
 #include <new>
+#include <utility>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -28,6 +32,25 @@ using namespace isspa;
 namespace {
 
 constexpr int kStepsPerGraph = 8;
+
+// Page-locked buffers handed out by isspa_host_alloc and not yet freed:
+// host start -> (bytes, device address of the start).
+std::mutex g_host_mu;
+std::map<uintptr_t, std::pair<size_t, uintptr_t>> g_host_bufs;
+
+// Device address of the host range [p, p + bytes) when it is 16-byte aligned
+// and lies inside one live isspa_host_alloc buffer; nullptr otherwise (any
+// other memory is only ever reached through cudaMemcpyAsync).
+void *host_mapped(const void *p, size_t bytes) {
+    const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+    if (!p || a % 16) return nullptr;
+    std::lock_guard<std::mutex> lock(g_host_mu);
+    auto it = g_host_bufs.upper_bound(a);
+    if (it == g_host_bufs.begin()) return nullptr;
+    --it;
+    if (a - it->first > it->second.first || bytes > it->second.first - (a - it->first)) return nullptr;
+    return reinterpret_cast<void *>(it->second.second + (a - it->first));
+}
 
 struct Fail {
     int code;
@@ -1332,16 +1355,28 @@ int isspa_time_steps_detailed(isspa_engine *e, int nsteps, size_t flush_bytes, d
 
 int isspa_host_alloc(size_t bytes, void **out) {
     if (!out || !bytes) return ISSPA_ERR_ARG;
-    if (cudaMallocHost(out, bytes) != cudaSuccess) {
+    if (cudaHostAlloc(out, bytes, cudaHostAllocPortable | cudaHostAllocMapped) != cudaSuccess) {
         cudaGetLastError();
         *out = nullptr;
         return ISSPA_ERR_NOMEM;
+    }
+    void *dev = nullptr;
+    if (cudaHostGetDevicePointer(&dev, *out, 0) == cudaSuccess && dev) {
+        std::lock_guard<std::mutex> lock(g_host_mu);
+        g_host_bufs[reinterpret_cast<uintptr_t>(*out)] = {bytes, reinterpret_cast<uintptr_t>(dev)};
+    } else {
+        cudaGetLastError();  // not mapped: isspa_step_host copies it instead
     }
     return ISSPA_OK;
 }
 
 void isspa_host_free(void *p) {
-    if (p) cudaFreeHost(p);
+    if (!p) return;
+    {
+        std::lock_guard<std::mutex> lock(g_host_mu);
+        g_host_bufs.erase(reinterpret_cast<uintptr_t>(p));
+    }
+    cudaFreeHost(p);
 }
 
 int isspa_synchronize(isspa_engine *e) {
@@ -1432,13 +1467,32 @@ int isspa_step_host(isspa_engine *e, const float *pin, const float *vin, float *
     int rc = guard(e);
     if (rc) return rc;
     const size_t b = sizeof(float4) * e->n_atoms;
+    // Buffers that all come from isspa_host_alloc are read and written by two
+    // small kernels around the step (the GPU reaches page-locked host memory
+    // directly); anything else goes through one copy per buffer.
+    const auto *dpin = static_cast<const float4 *>(host_mapped(pin, b));
+    const auto *dvin = static_cast<const float4 *>(host_mapped(vin, b));
+    auto *dpout = static_cast<float4 *>(host_mapped(pout, b));
+    auto *dvout = static_cast<float4 *>(host_mapped(vout, b));
+    auto *dfout = static_cast<float4 *>(host_mapped(fout, b));
+    const bool direct = (!pin || dpin) && (!vin || dvin) && (!pout || dpout) && (!vout || dvout) && (!fout || dfout);
     return run_guarded([&] {
-        if (pin) ck(cudaMemcpyAsync(e->pos, pin, b, cudaMemcpyHostToDevice, e->stream));
-        if (vin) ck(cudaMemcpyAsync(e->vel, vin, b, cudaMemcpyHostToDevice, e->stream));
-        e->run_steps(1);
-        if (pout) ck(cudaMemcpyAsync(pout, e->pos, b, cudaMemcpyDeviceToHost, e->stream));
-        if (vout) ck(cudaMemcpyAsync(vout, e->vel, b, cudaMemcpyDeviceToHost, e->stream));
-        if (fout) ck(cudaMemcpyAsync(fout, e->force_out, b, cudaMemcpyDeviceToHost, e->stream));
+        if (direct) {
+            if (pin || vin) launch_copy3(Copy3Args{{dpin, dvin, nullptr}, {e->pos, e->vel, nullptr}, e->n_atoms}, e->stream);
+            e->run_steps(1);
+            if (pout || vout || fout)
+                launch_copy3(Copy3Args{{pout ? e->pos : nullptr, vout ? e->vel : nullptr, fout ? e->force_out : nullptr},
+                                       {dpout, dvout, dfout}, e->n_atoms},
+                             e->stream);
+            ck(cudaGetLastError());
+        } else {
+            if (pin) ck(cudaMemcpyAsync(e->pos, pin, b, cudaMemcpyHostToDevice, e->stream));
+            if (vin) ck(cudaMemcpyAsync(e->vel, vin, b, cudaMemcpyHostToDevice, e->stream));
+            e->run_steps(1);
+            if (pout) ck(cudaMemcpyAsync(pout, e->pos, b, cudaMemcpyDeviceToHost, e->stream));
+            if (vout) ck(cudaMemcpyAsync(vout, e->vel, b, cudaMemcpyDeviceToHost, e->stream));
+            if (fout) ck(cudaMemcpyAsync(fout, e->force_out, b, cudaMemcpyDeviceToHost, e->stream));
+        }
         ck(cudaStreamSynchronize(e->stream));
     });
 }

@@ -434,6 +434,18 @@ void launch_cell_index(const float4 *pos, int off, int n, float rc, int3 nc, int
     if (n > 0) cell_index_kernel<<<(n + 127) / 128, 128, 0, s>>>(pos, off, n, rc, nc, cell);
 }
 
+__global__ void copy3_kernel(Copy3Args a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+        if (a.src[k]) a.dst[k][i] = a.src[k][i];
+}
+
+void launch_copy3(const Copy3Args &a, cudaStream_t s) {
+    if (a.n > 0) copy3_kernel<<<(a.n + 255) / 256, 256, 0, s>>>(a);
+}
+
 double measure_fp32_peak_tflops() {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);

@@ -198,6 +198,15 @@ void launch_bonded(const BondedArgs &a, cudaStream_t s);
 void launch_umbrella(const UmbrellaArgs &a, cudaStream_t s);
 void launch_leapfrog(const LeapfrogArgs &a, cudaStream_t s);
 void launch_neighbor_list(const ListArgs &a, cudaStream_t s);
+// Up to three float4 arrays of n elements copied element-wise (a null source
+// skips its pair): state moved between the engine's device arrays and
+// page-locked host buffers that the GPU reads and writes directly.
+struct Copy3Args {
+    const float4 *src[3];
+    float4 *dst[3];
+    int n;
+};
+void launch_copy3(const Copy3Args &a, cudaStream_t s);
 void launch_cell_index(const float4 *pos, int atom_off, int n, float rc, int3 ncell, int *cell,
                        cudaStream_t s);
 double measure_fp32_peak_tflops();

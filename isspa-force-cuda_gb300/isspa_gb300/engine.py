@@ -7,6 +7,7 @@ force accumulator exactly as the reference kernels add into for_d.
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 from typing import Iterable, Optional, Sequence
 
 import numpy as np
@@ -183,7 +184,18 @@ class Engine:
         return com, cv
 
     def step_host(self, pos_in, vel_in, pos_out, vel_out, force_out):
-        args = [_ptr(a) if a is not None else None for a in (pos_in, vel_in, pos_out, vel_out, force_out)]
+        """One step through isspa_step_host.  Each argument is None or a
+        C-contiguous float32 array of n_atoms x 4 (outputs writeable); arrays
+        from host_array are read and written by the GPU directly."""
+        args = []
+        for k, a in enumerate((pos_in, vel_in, pos_out, vel_out, force_out)):
+            if a is None:
+                args.append(None)
+                continue
+            if (a.dtype != np.float32 or a.size != 4 * self.n_atoms or not a.flags.c_contiguous
+                    or (k >= 2 and not a.flags.writeable)):
+                raise ValueError("step_host buffers: C-contiguous float32 arrays of n_atoms x 4, outputs writeable")
+            args.append(a.ctypes.data)
         abi.check(abi.lib().isspa_step_host(self._h, *args), "step_host")
 
     # ----------------------------------------------------------- MC points
@@ -252,6 +264,19 @@ class Engine:
         cell = np.zeros(self.windows[0].n_atoms, np.int32)
         abi.check(abi.lib().isspa_cell_list(self._h, float(rc), _ptr(nc), _ptr(cell)), "cell list")
         return cell
+
+
+def host_array(shape, dtype=np.float32) -> np.ndarray:
+    """A numpy array in page-locked, device-mapped memory (isspa_host_alloc),
+    released through isspa_host_free once no view of it is left.  Engine.step_host
+    with such arrays lets the GPU read and write them directly."""
+    dt = np.dtype(dtype)
+    nbytes = int(np.prod(shape)) * dt.itemsize
+    p = C.c_void_p()
+    abi.check(abi.lib().isspa_host_alloc(nbytes, C.byref(p)), "host alloc")
+    buf = (C.c_char * nbytes).from_address(p.value)
+    weakref.finalize(buf, abi.lib().isspa_host_free, C.c_void_p(p.value))
+    return np.frombuffer(buf, dtype=dt).reshape(shape)
 
 
 def measure_fp32_peak() -> float:
