@@ -111,6 +111,8 @@ typedef struct isspa_engine_options {
     size_t mem_cap;      /* device bytes the engine may hold, including the temporary
                             buffers of the list queries; 0 => unlimited */
     int force_atoms_per_thread;  /* receiving atoms per IS-SPA force thread, 1 or 2; 0 => 1 */
+    int force_tail_chunk;  /* MC points per force work item of the short items listed after
+                              all force_chunk items (about two waves of them); 0 => none */
 } isspa_engine_options;
 
 #define ISSPA_TERMS_NONE (-1)
@@ -171,12 +173,14 @@ int isspa_engine_info(const isspa_engine *e, int *n_windows, int *n_atoms_total,
  * shape[0] field atom-loop split, [1] field tiles, [2] force points per work
  * item, [3] force work items, [4] nonbond work items, [5] nonbond partners per
  * item, [6] SM count used for the choice, [7] receiving atoms per force
- * thread. */
-#define ISSPA_SHAPE_COUNT 8
+ * thread, [8] points per force work item of the short items listed last (0:
+ * none). */
+#define ISSPA_SHAPE_COUNT 9
 int isspa_engine_shapes(const isspa_engine *e, int shape[ISSPA_SHAPE_COUNT]);
 /* Autotuner: times every field-pass atom split and, for 1 and 2 receiving
  * atoms per force thread, a set of force-pass chunk lengths (those filling
- * 1..12 whole waves of resident blocks, and powers of two) on this engine's own
+ * 1..12 whole waves of resident blocks, and powers of two; and long chunks
+ * followed by about two waves of short ones) on this engine's own
  * workload with CUDA events (reps launches each), keeps the fastest of each
  * and reports the result as isspa_engine_shapes does.  Clears the force
  * accumulator; invalidates captured graphs. */

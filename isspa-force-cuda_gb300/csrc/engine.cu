@@ -88,6 +88,7 @@ struct isspa_engine {
     int4 *force_items = nullptr;
     int2 *force_chunks = nullptr;
     int n_force_items = 0, force_chunk = 0;
+    int force_tail = 0;  // chunk length of the short items listed last (0: none)
     int force_apt = 1;  // receiving atoms per force-kernel thread (1 or 2)
     int4 *nb_items = nullptr;
     int *nb_nj = nullptr;
@@ -225,28 +226,48 @@ struct isspa_engine {
         n_field_tiles = (int)t.size();
         field_split = S;
     }
-    void set_force_chunk(int C) {
-        std::vector<int4> items;
-        std::vector<int2> chunks;
-        for (int w : order) {
-            const WinDev &d = win_h[w];
-            const long long P = (long long)d.n_atoms * n_mc;
-            const int c0 = (int)chunks.size();
-            for (long long p = 0; p < P; p += C)
-                chunks.push_back(make_int2((int)(d.point_off + p), (int)std::min<long long>(C, P - p)));
-            const int nc = (int)chunks.size() - c0;
-            // chunk-major: blocks that run together read the same point records
-            // and add into different atom tiles' accumulators
-            for (int c = 0; c < nc; ++c)
-                for (int a = 0; a < d.n_atoms; a += 128)
-                    items.push_back(make_int4(w, d.atom_off + a, std::min(128, d.n_atoms - a), c0 + c));
+    // Force work items: C-point chunks of every window, then (Ct > 0) the last
+    // stretch of every window's points in Ct-point chunks, listed after all
+    // the long items.  Each item carries a fixed set-up cost (about 2.5 points'
+    // worth), so long chunks are cheaper, while the grid's last blocks set
+    // the tail; short items at the end fill the SMs the long ones free.  The
+    // short stretch is sized to about two waves of resident blocks.
+    void set_force_chunk(int C, int Ct = 0) {
+        if (Ct >= C) Ct = 0;
+        double f = 0.0;  // fraction of each window's points in short chunks
+        if (Ct > 0) {
+            const long long slots = (long long)n_sms * std::max(1, force_blocks_per_sm(force_apt));
+            double point_tiles = 0.0;
+            for (const WinDev &d : win_h) point_tiles += (double)d.n_atoms * n_mc * ((d.n_atoms + 127) / 128);
+            f = std::min(1.0, 2.0 * (double)slots * Ct / std::max(point_tiles, 1.0));
         }
+        std::vector<int4> items, tail;
+        std::vector<int2> chunks;
+        // chunk-major: blocks that run together read the same point records
+        // and add into different atom tiles' accumulators
+        auto add = [&](std::vector<int4> &out, int w, long long p0, long long p1, int len) {
+            const WinDev &d = win_h[w];
+            const int c0 = (int)chunks.size();
+            for (long long p = p0; p < p1; p += len)
+                chunks.push_back(make_int2((int)(d.point_off + p), (int)std::min<long long>(len, p1 - p)));
+            for (int c = c0; c < (int)chunks.size(); ++c)
+                for (int a = 0; a < d.n_atoms; a += 128)
+                    out.push_back(make_int4(w, d.atom_off + a, std::min(128, d.n_atoms - a), c));
+        };
+        for (int w : order) {
+            const long long P = (long long)win_h[w].n_atoms * n_mc;
+            const long long tp = Ct > 0 ? std::min<long long>(P, std::llround(f * (double)P / Ct) * Ct) : 0;
+            add(items, w, 0, P - tp, C);
+            if (tp > 0) add(tail, w, P - tp, P, Ct);
+        }
+        items.insert(items.end(), tail.begin(), tail.end());
         release(force_items);
         release(force_chunks);
         force_items = upload(items);
         force_chunks = upload(chunks);
         n_force_items = (int)items.size();
         force_chunk = C;
+        force_tail = Ct;
     }
 
     ~isspa_engine() {
@@ -712,7 +733,8 @@ void build(isspa_engine &E, const std::vector<isspa_host_system> &ws) {
     if (S != 1 && S != 2 && S != 4 && S != 8 && S != 16) S = E.default_field_split();
     E.set_field_split(S);
     E.force_apt = E.opt.force_atoms_per_thread == 2 ? 2 : 1;
-    E.set_force_chunk(E.opt.force_chunk > 0 ? E.opt.force_chunk : E.default_force_chunk());
+    E.set_force_chunk(E.opt.force_chunk > 0 ? E.opt.force_chunk : E.default_force_chunk(),
+                      std::max(0, E.opt.force_tail_chunk));
     // nonbond items: 128 i-atoms x J partners
     std::vector<int4> nitems;
     std::vector<int> nnj;
@@ -934,6 +956,7 @@ int isspa_engine_shapes(const isspa_engine *e, int shape[ISSPA_SHAPE_COUNT]) {
     shape[5] = e->nb_chunk;
     shape[6] = e->n_sms;
     shape[7] = e->force_apt;
+    shape[8] = e->force_tail;
     return ISSPA_OK;
 }
 
@@ -1199,7 +1222,7 @@ int isspa_autotune(isspa_engine *e, int reps, int shape[ISSPA_SHAPE_COUNT]) {
         long long maxP = 0;
         for (const WinDev &d : e->win_h) maxP = std::max(maxP, (long long)d.n_atoms * e->n_mc);
         best = 1e30f;
-        int bestC = e->force_chunk, bestA = e->force_apt;
+        int bestC = e->force_chunk, bestT = e->force_tail, bestA = e->force_apt;
         for (int apt : {1, 2}) {
             e->force_apt = apt;
             const long long slots = (long long)e->n_sms * std::max(1, force_blocks_per_sm(apt));
@@ -1217,18 +1240,26 @@ int isspa_autotune(isspa_engine *e, int reps, int shape[ISSPA_SHAPE_COUNT]) {
                 if (c <= std::max<long long>(128, maxP)) cands.push_back(c);
             std::sort(cands.begin(), cands.end());
             cands.erase(std::unique(cands.begin(), cands.end()), cands.end());
-            for (int c : cands) {
-                e->set_force_chunk(c);
+            // (long chunk, short tail chunk) pairs: long items first, then about
+            // two waves of short ones
+            std::vector<std::pair<int, int>> pairs;
+            for (int c : cands) pairs.push_back({c, 0});
+            for (int c : {64, 128, 256, 512, 1024})
+                for (int t : {16, 32, 64})
+                    if (t < c && c <= std::max<long long>(128, maxP)) pairs.push_back({c, t});
+            for (const auto &ct : pairs) {
+                e->set_force_chunk(ct.first, ct.second);
                 const float ms = time_it([&] { launch_force(e->force_args(), e->stream); });
                 if (ms < best) {
                     best = ms;
-                    bestC = c;
+                    bestC = ct.first;
+                    bestT = ct.second;
                     bestA = apt;
                 }
             }
         }
         e->force_apt = bestA;
-        e->set_force_chunk(bestC);
+        e->set_force_chunk(bestC, bestT);
         ck(cudaMemsetAsync(e->facc, 0, 3 * sizeof(unsigned long long) * e->n_atoms, e->stream));
         ck(cudaStreamSynchronize(e->stream));
         e->invalidate_graphs();

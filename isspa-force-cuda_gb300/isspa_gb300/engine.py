@@ -23,7 +23,8 @@ def _ptr(a: np.ndarray):
 class Engine:
     def __init__(self, windows: "System | Sequence[System]", isspa_terms: int = 7,
                  nonbond_terms: int = 7, use_graph: bool = True, field_split: int = 0,
-                 force_chunk: int = 0, mem_cap: int = 0, force_atoms_per_thread: int = 0):
+                 force_chunk: int = 0, mem_cap: int = 0, force_atoms_per_thread: int = 0,
+                 force_tail_chunk: int = 0):
         if isinstance(windows, System):
             windows = [windows]
         self.windows = list(windows)
@@ -40,6 +41,7 @@ class Engine:
         opt.use_graph, opt.field_split, opt.force_chunk = int(use_graph), int(field_split), int(force_chunk)
         opt.mem_cap = int(mem_cap)
         opt.force_atoms_per_thread = int(force_atoms_per_thread)
+        opt.force_tail_chunk = int(force_tail_chunk)
         h = C.c_void_p()
         abi.check(L.isspa_engine_create(descs, len(self.windows), C.byref(opt), C.byref(h)), "engine create")
         self._h = h
@@ -52,7 +54,7 @@ class Engine:
         v = (C.c_int * abi.SHAPE_COUNT)()
         abi.check(abi.lib().isspa_engine_shapes(self._h, v), "shapes")
         keys = ("field_split", "field_tiles", "force_chunk", "force_items", "nonbond_items",
-                "nonbond_partners_per_item", "sms", "force_atoms_per_thread")
+                "nonbond_partners_per_item", "sms", "force_atoms_per_thread", "force_tail_chunk")
         return dict(zip(keys, list(v)))
 
     def autotune(self, reps: int = 3) -> dict:

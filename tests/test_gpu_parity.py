@@ -185,14 +185,15 @@ def test_graph_step_equals_call_sequence(synth_medium):
     assert a.get_step() == 10
 
 
-@pytest.mark.parametrize("chunk", [128, 37])
-def test_force_kernel_atoms_per_thread_bit_identical(synth_medium, chunk):
+@pytest.mark.parametrize("chunk, tail", [(128, 0), (37, 0), (256, 32)])
+def test_force_kernel_atoms_per_thread_bit_identical(synth_medium, chunk, tail):
     """With the same point chunks, the 2-atoms-per-thread force kernel gives the
     1-atom kernel's forces bit for bit (each atom sees the same arithmetic in
-    the same order), also with a ragged chunk and partial atom tiles."""
+    the same order), also with a ragged chunk, partial atom tiles and short
+    chunks listed last."""
     out = []
     for apt in (1, 2):
-        eng = ig.Engine(synth_medium, force_atoms_per_thread=apt, force_chunk=chunk)
+        eng = ig.Engine(synth_medium, force_atoms_per_thread=apt, force_chunk=chunk, force_tail_chunk=tail)
         assert eng.shapes()["force_atoms_per_thread"] == apt
         eng.zero_forces()
         eng.isspa_force()
@@ -201,6 +202,29 @@ def test_force_kernel_atoms_per_thread_bit_identical(synth_medium, chunk):
         out.append(eng.positions())
     assert np.array_equal(out[0], out[2])
     assert np.array_equal(out[1], out[3])
+
+
+@pytest.mark.parametrize("chunk, tail", [(512, 32), (128, 16), (64, 0)])
+def test_force_work_list_with_short_items_last(synth_medium, chunk, tail):
+    """Long chunks followed by short ones cover every (atom, point) pair once:
+    the IS-SPA force matches the oracle, and the item count is that of the two
+    chunk lengths."""
+    s = synth_medium
+    eng = ig.Engine(s, force_chunk=chunk, force_tail_chunk=tail)
+    sh = eng.shapes()
+    assert sh["force_chunk"] == chunk and sh["force_tail_chunk"] == tail
+    tiles = -(-s.n_atoms // 128)
+    P = s.n_atoms * s.n_mc
+    if tail == 0:
+        assert sh["force_items"] == tiles * -(-P // chunk)
+    else:
+        n_long = (sh["force_items"] // tiles)  # chunks of both lengths
+        assert sh["force_items"] % tiles == 0 and n_long > -(-P // chunk)
+    eng.zero_forces()
+    eng.isspa_force()
+    o = O.Oracle(s)
+    ref = o.isspa_force(o.mc_points(seed=s.seed, step=0), terms=7)
+    assert nrel(eng.forces(), ref) < FORCE_TOL
 
 
 def test_point_injection(adi2_100):
