@@ -92,6 +92,8 @@ __global__ void __launch_bounds__(FieldShape<S>::kThreads) field_kernel(FieldArg
     __shared__ float4 s_atom[kT];
     __shared__ int s_row[kT];
     __shared__ float s_red[S > 1 ? 8 : 1][kT];
+    constexpr bool kShareDraws = GEN && S >= 4;
+    __shared__ float s_pt[3][kShareDraws ? kT / S : 1];  // the block's points, drawn once
 
     const int4 tile = a.tiles[blockIdx.x];
     const WinDev W = a.win[tile.x];
@@ -108,7 +110,23 @@ __global__ void __launch_bounds__(FieldShape<S>::kThreads) field_kernel(FieldArg
     const float L = W.box, h = W.hbox;
 
     float px, py, pz;
-    if (GEN) {
+    if (kShareDraws) {
+        // one warp of each group draws the group's 32 points (rejection
+        // sampling, divergent attempt counts); the other S-1 warps wait at the
+        // barrier instead of repeating the draws on issue slots the SM needs
+        // (1100 atoms, S = 8: 0.0876 against 0.0925 ms per launch; with S = 2
+        // the barrier costs more than the one repeated draw saves)
+        if (sp == 0) {
+            mc_point((uint32_t)pw, (uint32_t)tile.x, *a.step_ptr, a.seed_lo, a.seed_hi, xo, rm, px, py, pz);
+            s_pt[0][slot] = px;
+            s_pt[1][slot] = py;
+            s_pt[2][slot] = pz;
+        }
+        __syncthreads();
+        px = s_pt[0][slot];
+        py = s_pt[1][slot];
+        pz = s_pt[2][slot];
+    } else if (GEN) {
         mc_point((uint32_t)pw, (uint32_t)tile.x, *a.step_ptr, a.seed_lo, a.seed_hi, xo, rm, px, py, pz);
     } else {
         px = a.pts_in[3 * pg + 0];
