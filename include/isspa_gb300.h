@@ -113,6 +113,9 @@ typedef struct isspa_engine_options {
     int force_atoms_per_thread;  /* receiving atoms per IS-SPA force thread, 1 or 2; 0 => 1 */
     int force_tail_chunk;  /* MC points per force work item of the short items listed after
                               all force_chunk items (about two waves of them); 0 => none */
+    int field_vote;      /* 1: the field pass walks its atoms in groups of four with one
+                            warp vote on "any inside rmax" per group (same results);
+                            0 => per-pair branches */
 } isspa_engine_options;
 
 #define ISSPA_TERMS_NONE (-1)
@@ -174,10 +177,11 @@ int isspa_engine_info(const isspa_engine *e, int *n_windows, int *n_atoms_total,
  * item, [3] force work items, [4] nonbond work items, [5] nonbond partners per
  * item, [6] SM count used for the choice, [7] receiving atoms per force
  * thread, [8] points per force work item of the short items listed last (0:
- * none). */
-#define ISSPA_SHAPE_COUNT 9
+ * none), [9] 1 when the field pass walks its atoms in warp-voted groups. */
+#define ISSPA_SHAPE_COUNT 10
 int isspa_engine_shapes(const isspa_engine *e, int shape[ISSPA_SHAPE_COUNT]);
-/* Autotuner: times every field-pass atom split and, for 1 and 2 receiving
+/* Autotuner: times every field-pass atom split (per-pair and warp-voted
+ * loops) and, for 1 and 2 receiving
  * atoms per force thread, a set of force-pass chunk lengths (those filling
  * 1..12 whole waves of resident blocks, and powers of two; and long chunks
  * followed by about two waves of short ones) on this engine's own

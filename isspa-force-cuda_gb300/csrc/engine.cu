@@ -89,6 +89,7 @@ struct isspa_engine {
     int2 *force_chunks = nullptr;
     int n_force_items = 0, force_chunk = 0;
     int force_tail = 0;  // chunk length of the short items listed last (0: none)
+    int field_vote = 0;  // field pass in warp-voted groups of four atoms
     int force_apt = 1;  // receiving atoms per force-kernel thread (1 or 2)
     int4 *nb_items = nullptr;
     int *nb_nj = nullptr;
@@ -288,6 +289,7 @@ struct isspa_engine {
     // ---------------------------------------------------------------- args
     FieldArgs field_args() const {
         FieldArgs a{};
+        a.vote = field_vote;
         a.pos = pos;
         a.atype = atype;
         a.win = win;
@@ -732,6 +734,7 @@ void build(isspa_engine &E, const std::vector<isspa_host_system> &ws) {
     int S = E.opt.field_split;
     if (S != 1 && S != 2 && S != 4 && S != 8 && S != 16) S = E.default_field_split();
     E.set_field_split(S);
+    E.field_vote = E.opt.field_vote == 1 ? 1 : 0;
     E.force_apt = E.opt.force_atoms_per_thread == 2 ? 2 : 1;
     E.set_force_chunk(E.opt.force_chunk > 0 ? E.opt.force_chunk : E.default_force_chunk(),
                       std::max(0, E.opt.force_tail_chunk));
@@ -957,6 +960,7 @@ int isspa_engine_shapes(const isspa_engine *e, int shape[ISSPA_SHAPE_COUNT]) {
     shape[6] = e->n_sms;
     shape[7] = e->force_apt;
     shape[8] = e->force_tail;
+    shape[9] = e->field_vote;
     return ISSPA_OK;
 }
 
@@ -1204,18 +1208,22 @@ int isspa_autotune(isspa_engine *e, int reps, int shape[ISSPA_SHAPE_COUNT]) {
             ck(cudaEventElapsedTime(&ms, e->ev_a, e->ev_b));
             return ms / reps;
         };
-        // field pass: every atom-loop split
+        // field pass: every atom-loop split, per-pair and warp-voted loops
         float best = 1e30f;
-        int bestS = e->field_split;
-        for (int S : {1, 2, 4, 8, 16}) {
-            e->set_field_split(S);
-            const float ms = time_it([&] { launch_field(e->field_args(), S, false, e->stream); });
-            if (ms < best) {
-                best = ms;
-                bestS = S;
+        int bestS = e->field_split, bestV = e->field_vote;
+        for (int V : {0, 1})
+            for (int S : {1, 2, 4, 8, 16}) {
+                e->set_field_split(S);
+                e->field_vote = V;
+                const float ms = time_it([&] { launch_field(e->field_args(), S, false, e->stream); });
+                if (ms < best) {
+                    best = ms;
+                    bestS = S;
+                    bestV = V;
+                }
             }
-        }
         e->set_field_split(bestS);
+        e->field_vote = bestV;
         launch_field(e->field_args(), bestS, false, e->stream);
         // force pass: for 1 and 2 atoms per thread, the chunk lengths that fill
         // 1..12 whole waves of that kernel's resident blocks, and powers of two

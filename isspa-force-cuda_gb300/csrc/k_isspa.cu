@@ -86,7 +86,9 @@ struct FieldShape {
     static constexpr int kThreads = S >= 4 ? 32 * S : kFieldThreads;  // kThreads/(32 S) point groups
 };
 
-template <int S, bool GEN, bool RAW>
+// VOTE: the atom loop takes groups of four atoms and one warp vote per group
+// (see below); same operations in the same order as the per-pair loop.
+template <int S, bool GEN, bool RAW, bool VOTE>
 __global__ void __launch_bounds__(FieldShape<S>::kThreads) field_kernel(FieldArgs a) {
     constexpr int kT = FieldShape<S>::kThreads;
     __shared__ float4 s_atom[kT];
@@ -144,6 +146,51 @@ __global__ void __launch_bounds__(FieldShape<S>::kThreads) field_kernel(FieldArg
     const bool one_grid = g_r0 == e_r0 && g_dr == e_dr;
     const int nb = a.n_gbins;
 
+    // geometry of the pair (point, staged atom k); true when inside rmax of
+    // the owner's type (:154)
+    auto geom = [&](int k, float &rx, float &ry, float &rz, float &c) {
+        const float4 xj = s_atom[k];
+        rx = mimg(px - xj.x, L, h);
+        ry = mimg(py - xj.y, L, h);
+        rz = mimg(pz - xj.z, L, h);
+        const float d2 = dist2f(rx, ry, rz);
+        const float ri = rsqrtf(d2);
+        c = xj.w * (ri * ri * ri);
+        return d2 <= rm2;
+    };
+    // ex.. accumulates the in-range contributions (Coulomb and tabulated
+    // field), fx.. the out-of-range Coulomb field E0; E = ex.. + fx..  d2 and
+    // ri are recomputed from the same operands (same values) to keep fewer
+    // registers live across a group.
+    auto accum = [&](int k, float rx, float ry, float rz, float c) {
+        const float d2 = dist2f(rx, ry, rz);
+        if (d2 <= rm2) {
+            const float ri = rsqrtf(d2);
+            ++n;
+            ex = fmaf(-c, rx, ex);
+            ey = fmaf(-c, ry, ey);
+            ez = fmaf(-c, rz, ez);
+            const float dist = one_grid ? density_table_dist(d2, ri) : __fsqrt_rn(d2);
+            const int bin = (int)__fmul_rn(__fsub_rn(dist, g_r0), g_inv);
+            if (bin < 0) {
+                w = 0.0f;
+            } else if (bin < nb) {
+                const float4 t = __ldg(a.gtab + s_row[k] + bin);
+                const float fg = (dist - fmaf((float)bin, g_dr, g_r0)) * g_inv;
+                w *= fmaf(fg, t.y - t.x, t.x);
+                const float fe = (dist - fmaf((float)bin, e_dr, e_r0)) * e_inv;
+                const float et = fmaf(fe, t.w - t.z, t.z) * ri;
+                ex = fmaf(et, rx, ex);
+                ey = fmaf(et, ry, ey);
+                ez = fmaf(et, rz, ez);
+            }
+        } else {
+            fx = fmaf(-c, rx, fx);
+            fy = fmaf(-c, ry, fy);
+            fz = fmaf(-c, rz, fz);
+        }
+    };
+
     for (int j0 = 0; j0 < W.n_atoms; j0 += kT) {
         const int jn = min(kT, W.n_atoms - j0);
         __syncthreads();
@@ -155,40 +202,46 @@ __global__ void __launch_bounds__(FieldShape<S>::kThreads) field_kernel(FieldArg
             s_row[threadIdx.x] = a.atype[j].y * nb;
         }
         __syncthreads();
-#pragma unroll 4
-        for (int k = sp; k < jn; k += S) {
-            const float4 xj = s_atom[k];
-            const float rx = mimg(px - xj.x, L, h);
-            const float ry = mimg(py - xj.y, L, h);
-            const float rz = mimg(pz - xj.z, L, h);
-            const float d2 = dist2f(rx, ry, rz);
-            const float ri = rsqrtf(d2);
-            const float c = xj.w * (ri * ri * ri);
-            // ex.. accumulates the in-range contributions (Coulomb and tabulated
-            // field), fx.. the out-of-range Coulomb field E0; E = ex.. + fx..
-            if (d2 <= rm2) {  // inside rmax of the owner's type (:154)
-                ++n;
-                ex = fmaf(-c, rx, ex);
-                ey = fmaf(-c, ry, ey);
-                ez = fmaf(-c, rz, ez);
-                const float dist = one_grid ? density_table_dist(d2, ri) : __fsqrt_rn(d2);
-                const int bin = (int)__fmul_rn(__fsub_rn(dist, g_r0), g_inv);
-                if (bin < 0) {
-                    w = 0.0f;
-                } else if (bin < nb) {
-                    const float4 t = __ldg(a.gtab + s_row[k] + bin);
-                    const float fg = (dist - fmaf((float)bin, g_dr, g_r0)) * g_inv;
-                    w *= fmaf(fg, t.y - t.x, t.x);
-                    const float fe = (dist - fmaf((float)bin, e_dr, e_r0)) * e_inv;
-                    const float et = fmaf(fe, t.w - t.z, t.z) * ri;
-                    ex = fmaf(et, rx, ex);
-                    ey = fmaf(et, ry, ey);
-                    ez = fmaf(et, rz, ez);
-                }
+        int k = sp;
+        // Groups of kG staged atoms: one warp vote tells whether any lane has
+        // any of them inside rmax.  When none does, their out-of-range Coulomb
+        // terms are summed without per-pair branches; the accumulators see the
+        // same operations in the same order either way.  It pays where few
+        // groups have an atom in range (large systems: 16 384 atoms in a
+        // 120 A box, 21.5 against 23.4 ms per launch) and costs registers
+        // where many do (1100 atoms: 0.092 against 0.087 ms), so the
+        // autotuner chooses.
+        constexpr int kG = 4;
+        for (; VOTE && k + (kG - 1) * S < jn; k += kG * S) {
+            float rx[kG], ry[kG], rz[kG], c[kG];
+            bool any = false;
+#pragma unroll
+            for (int u = 0; u < kG; ++u) any = geom(k + u * S, rx[u], ry[u], rz[u], c[u]) || any;
+            if (__any_sync(0xffffffffu, any)) {
+#pragma unroll
+                for (int u = 0; u < kG; ++u) accum(k + u * S, rx[u], ry[u], rz[u], c[u]);
             } else {
-                fx = fmaf(-c, rx, fx);
-                fy = fmaf(-c, ry, fy);
-                fz = fmaf(-c, rz, fz);
+#pragma unroll
+                for (int u = 0; u < kG; ++u) {
+                    fx = fmaf(-c[u], rx[u], fx);
+                    fy = fmaf(-c[u], ry[u], fy);
+                    fz = fmaf(-c[u], rz[u], fz);
+                }
+            }
+        }
+        if (VOTE) {
+#pragma unroll 1
+            for (; k < jn; k += S) {  // at most kG - 1 atoms
+                float rx, ry, rz, c;
+                geom(k, rx, ry, rz, c);
+                accum(k, rx, ry, rz, c);
+            }
+        } else {
+#pragma unroll 4
+            for (; k < jn; k += S) {
+                float rx, ry, rz, c;
+                geom(k, rx, ry, rz, c);
+                accum(k, rx, ry, rz, c);
             }
         }
     }
@@ -382,15 +435,20 @@ __global__ void __launch_bounds__(ForceShape<A>::kThreads, ForceShape<A>::kMinBl
     }
 }
 
-template <int S, bool GEN, bool RAW>
+template <int S, bool GEN, bool RAW, bool VOTE = false>
 void launch_field_t(const FieldArgs &a, cudaStream_t s) {
-    field_kernel<S, GEN, RAW><<<a.n_tiles, FieldShape<S>::kThreads, 0, s>>>(a);
+    field_kernel<S, GEN, RAW, VOTE><<<a.n_tiles, FieldShape<S>::kThreads, 0, s>>>(a);
 }
 
 template <int S>
 void launch_field_s(const FieldArgs &a, bool raw, cudaStream_t s) {
     const bool gen = a.pts_in == nullptr;
-    if (gen && !raw) launch_field_t<S, true, false>(a, s);
+    // the vote variant gives the same results; the raw-field captures (tests,
+    // adjoint) always take the per-pair loop
+    if (a.vote && !raw) {
+        if (gen) launch_field_t<S, true, false, true>(a, s);
+        else launch_field_t<S, false, false, true>(a, s);
+    } else if (gen && !raw) launch_field_t<S, true, false>(a, s);
     else if (gen && raw) launch_field_t<S, true, true>(a, s);
     else if (!gen && !raw) launch_field_t<S, false, false>(a, s);
     else launch_field_t<S, false, true>(a, s);
@@ -399,7 +457,7 @@ void launch_field_s(const FieldArgs &a, bool raw, cudaStream_t s) {
 template <int S>
 int field_bps() {
     int n = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, field_kernel<S, true, false>, FieldShape<S>::kThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, field_kernel<S, true, false, false>, FieldShape<S>::kThreads, 0);
     return n;
 }
 

@@ -28,6 +28,7 @@ struct FieldArgs {
     float4 *raw_e0;        // optional: E0, n
     int terms;             // IS-SPA force terms: 1 multipole, 2 tabulated LJ, 4 CDD
     int *status;
+    int vote;              // 1: atom loop in warp-voted groups of four (same results)
 };
 
 // ---- IS-SPA force pass (one thread per receiving atom) -------------------

@@ -65,6 +65,23 @@ def test_mc_points_bit_identical(adi2_100):
     assert not np.array_equal(xyz17, xyz)
 
 
+@pytest.mark.parametrize("split", [1, 2, 4, 8, 16])
+def test_field_vote_loop_bit_identical(synth_medium, split):
+    """The warp-voted atom loop of the field pass gives the per-pair loop's
+    forces and trajectory bit for bit, at every atom-loop split."""
+    out = []
+    for vote in (0, 1):
+        eng = ig.Engine(synth_medium, field_split=split, field_vote=vote)
+        assert eng.shapes()["field_vote"] == vote and eng.shapes()["field_split"] == split
+        eng.zero_forces()
+        eng.isspa_force()
+        out.append(eng.forces())
+        eng.step(5)
+        out.append(eng.positions())
+    assert np.array_equal(out[0], out[2])
+    assert np.array_equal(out[1], out[3])
+
+
 @pytest.mark.parametrize("which", ["adi2", "medium", "medium-two-grids"])
 def test_field_matches_oracle(which, adi2_100, synth_medium):
     s = adi2_100 if which == "adi2" else synth_medium
