@@ -116,6 +116,9 @@ typedef struct isspa_engine_options {
     int field_vote;      /* 1: the field pass walks its atoms in groups of four with one
                             warp vote on "any inside rmax" per group (same results);
                             0 => per-pair branches */
+    int force_vote;      /* 1: the force pass (one atom per thread) takes its points in
+                            groups of four with one warp vote per group (same results);
+                            0 => per-pair branches */
 } isspa_engine_options;
 
 #define ISSPA_TERMS_NONE (-1)
@@ -177,14 +180,16 @@ int isspa_engine_info(const isspa_engine *e, int *n_windows, int *n_atoms_total,
  * item, [3] force work items, [4] nonbond work items, [5] nonbond partners per
  * item, [6] SM count used for the choice, [7] receiving atoms per force
  * thread, [8] points per force work item of the short items listed last (0:
- * none), [9] 1 when the field pass walks its atoms in warp-voted groups. */
-#define ISSPA_SHAPE_COUNT 10
+ * none), [9] 1 when the field pass walks its atoms in warp-voted groups,
+ * [10] 1 when the force pass takes its points in warp-voted groups. */
+#define ISSPA_SHAPE_COUNT 11
 int isspa_engine_shapes(const isspa_engine *e, int shape[ISSPA_SHAPE_COUNT]);
 /* Autotuner: times every field-pass atom split (per-pair and warp-voted
  * loops) and, for 1 and 2 receiving
  * atoms per force thread, a set of force-pass chunk lengths (those filling
  * 1..12 whole waves of resident blocks, and powers of two; and long chunks
- * followed by about two waves of short ones) on this engine's own
+ * followed by about two waves of short ones; then the voted force loop on the
+ * chosen list) on this engine's own
  * workload with CUDA events (reps launches each), keeps the fastest of each
  * and reports the result as isspa_engine_shapes does.  Clears the force
  * accumulator; invalidates captured graphs. */

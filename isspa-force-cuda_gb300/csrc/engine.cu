@@ -90,6 +90,7 @@ struct isspa_engine {
     int n_force_items = 0, force_chunk = 0;
     int force_tail = 0;  // chunk length of the short items listed last (0: none)
     int field_vote = 0;  // field pass in warp-voted groups of four atoms
+    int force_vote = 0;  // force pass in warp-voted groups of four points (1 atom per thread)
     int force_apt = 1;  // receiving atoms per force-kernel thread (1 or 2)
     int4 *nb_items = nullptr;
     int *nb_nj = nullptr;
@@ -319,6 +320,7 @@ struct isspa_engine {
     }
     ForceArgs force_args() const {
         ForceArgs a{};
+        a.vote = force_vote;
         a.pos = pos;
         a.atype = atype;
         a.win = win;
@@ -735,6 +737,7 @@ void build(isspa_engine &E, const std::vector<isspa_host_system> &ws) {
     if (S != 1 && S != 2 && S != 4 && S != 8 && S != 16) S = E.default_field_split();
     E.set_field_split(S);
     E.field_vote = E.opt.field_vote == 1 ? 1 : 0;
+    E.force_vote = E.opt.force_vote == 1 ? 1 : 0;
     E.force_apt = E.opt.force_atoms_per_thread == 2 ? 2 : 1;
     E.set_force_chunk(E.opt.force_chunk > 0 ? E.opt.force_chunk : E.default_force_chunk(),
                       std::max(0, E.opt.force_tail_chunk));
@@ -961,6 +964,7 @@ int isspa_engine_shapes(const isspa_engine *e, int shape[ISSPA_SHAPE_COUNT]) {
     shape[7] = e->force_apt;
     shape[8] = e->force_tail;
     shape[9] = e->field_vote;
+    shape[10] = e->force_apt == 1 ? e->force_vote : 0;
     return ISSPA_OK;
 }
 
@@ -1268,6 +1272,14 @@ int isspa_autotune(isspa_engine *e, int reps, int shape[ISSPA_SHAPE_COUNT]) {
         }
         e->force_apt = bestA;
         e->set_force_chunk(bestC, bestT);
+        // the voted force loop (one atom per thread) on the chosen work list
+        e->force_vote = 0;
+        if (bestA == 1) {
+            const float plain = time_it([&] { launch_force(e->force_args(), e->stream); });
+            e->force_vote = 1;
+            const float voted = time_it([&] { launch_force(e->force_args(), e->stream); });
+            e->force_vote = voted < plain ? 1 : 0;
+        }
         ck(cudaMemsetAsync(e->facc, 0, 3 * sizeof(unsigned long long) * e->n_atoms, e->stream));
         ck(cudaStreamSynchronize(e->stream));
         e->invalidate_graphs();

@@ -21,6 +21,8 @@
 //          final force is independent of scheduling order.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "kernels.h"
 #include "philox.h"
 
@@ -321,8 +323,15 @@ struct ForceShape {
     static constexpr int kMinBlocks = A == 1 ? 10 : 12;  // 48 / 85 registers per thread
 };
 
-template <bool LJ, int A>
-__global__ void __launch_bounds__(ForceShape<A>::kThreads, ForceShape<A>::kMinBlocks) force_kernel(ForceArgs a) {
+// VOTE (one atom per thread only): points in groups of four with one warp
+// vote per group on "any lane has any of them inside rmax"; a group with none
+// takes the out-of-range records without the per-pair select and tabulated-LJ
+// branch.  Same operations in the same order as the per-pair loop.  It keeps
+// four points' geometry live (64 registers, 8 blocks per SM).
+template <bool LJ, int A, bool VOTE = false>
+__global__ void __launch_bounds__(ForceShape<A>::kThreads, VOTE ? 8 : ForceShape<A>::kMinBlocks)
+    force_kernel(ForceArgs a) {
+    static_assert(!VOTE || A == 1, "the voted loop takes one receiving atom per thread");
     constexpr int kT = ForceShape<A>::kThreads;
     __shared__ PointRec s_p[kForceThreads];
     const int4 item = a.items[blockIdx.x];
@@ -370,48 +379,76 @@ __global__ void __launch_bounds__(ForceShape<A>::kThreads, ForceShape<A>::kMinBl
             s_p[i].q[4] = a.pts.q4[pg];
         }
         __syncthreads();
-#pragma unroll 4
-        for (int k = 0; k < pn; ++k) {
+        // the pair (staged point k, receiving atom u) after its geometry; FAR:
+        // the point is known to lie outside rmax of the atom's type
+        auto pair = [&](int k, int u, float rx, float ry, float rz, float d2, auto far) {
+            constexpr bool FAR = decltype(far)::value;
             const float4 *R = s_p[k].q;
-            const float4 P = R[0];
             const float4 E = R[1];
             const float4 K = R[2];
+            const bool inside = !FAR && d2 <= rm2[u];  // (:291)
+            const float ri = rsqrtf(d2);
+            const float ri2 = ri * ri;
+            const float ri3 = ri2 * ri;
+            const float ri5 = ri3 * ri2;
+            const float4 D = R[inside ? 3 : 4];
+            // multipole (:274-289) with the CDD term (:306-312) folded into D
+            const float w = fmaf(E.x, rx, fmaf(E.y, ry, E.z * rz));
+            const float dD = fmaf(D.x, rx, fmaf(D.y, ry, D.z * rz));
+            const float g = w * ri2;
+            float X = (w * g) * fmaf(K.y, g, K.x);
+            X = fmaf(3.0f, dD, X) - E.w;
+            X = fmaf(-K.w, g, X);
+            const float cR = X * ri5;
+            const float cE = fmaf(-D.w, ri2, fmaf(K.w, g, K.z) * g) * ri3;
+            qx[u] = fmaf(cR, rx, fmaf(-cE, E.x, fmaf(-ri3, D.x, qx[u])));
+            qy[u] = fmaf(cR, ry, fmaf(-cE, E.y, fmaf(-ri3, D.y, qy[u])));
+            qz[u] = fmaf(cR, rz, fmaf(-cE, E.z, fmaf(-ri3, D.z, qz[u])));
+            if (LJ && inside) {  // tabulated mean LJ force (:291-305)
+                const float dist = __fsqrt_rn(d2);
+                const int bin = (int)__fmaf_rn(__fsub_rn(dist, f_r0), f_inv, 0.5f);
+                if (bin >= 0 && bin < nf) {
+                    const float2 tv = __ldg(a.ftab + frow[u] + bin);
+                    const float fr = (dist - fmaf((float)bin, f_dr, f_r0)) * f_inv;
+                    const float fv = fmaf(fr, tv.y - tv.x, tv.x) * R[0].w * ri;
+                    lx[u] = fmaf(fv, rx, lx[u]);
+                    ly[u] = fmaf(fv, ry, ly[u]);
+                    lz[u] = fmaf(fv, rz, lz[u]);
+                }
+            }
+        };
+        int k = 0;
+        if (VOTE) {
+            for (; k + 3 < pn; k += 4) {
+                float rx[4], ry[4], rz[4], d2[4];
+                bool any = false;
+#pragma unroll
+                for (int v = 0; v < 4; ++v) {
+                    const float4 P = s_p[k + v].q[0];
+                    rx[v] = mimg(P.x - xi[0].x, L, h);
+                    ry[v] = mimg(P.y - xi[0].y, L, h);
+                    rz[v] = mimg(P.z - xi[0].z, L, h);
+                    d2[v] = dist2f(rx[v], ry[v], rz[v]);
+                    any = any || d2[v] <= rm2[0];
+                }
+                if (__any_sync(0xffffffffu, any)) {
+#pragma unroll
+                    for (int v = 0; v < 4; ++v) pair(k + v, 0, rx[v], ry[v], rz[v], d2[v], std::false_type{});
+                } else {
+#pragma unroll
+                    for (int v = 0; v < 4; ++v) pair(k + v, 0, rx[v], ry[v], rz[v], d2[v], std::true_type{});
+                }
+            }
+        }
+#pragma unroll 4
+        for (; k < pn; ++k) {
+            const float4 P = s_p[k].q[0];
 #pragma unroll
             for (int u = 0; u < A; ++u) {
                 const float rx = mimg(P.x - xi[u].x, L, h);
                 const float ry = mimg(P.y - xi[u].y, L, h);
                 const float rz = mimg(P.z - xi[u].z, L, h);
-                const float d2 = dist2f(rx, ry, rz);
-                const bool inside = d2 <= rm2[u];  // (:291)
-                const float ri = rsqrtf(d2);
-                const float ri2 = ri * ri;
-                const float ri3 = ri2 * ri;
-                const float ri5 = ri3 * ri2;
-                const float4 D = R[inside ? 3 : 4];
-                // multipole (:274-289) with the CDD term (:306-312) folded into D
-                const float w = fmaf(E.x, rx, fmaf(E.y, ry, E.z * rz));
-                const float dD = fmaf(D.x, rx, fmaf(D.y, ry, D.z * rz));
-                const float g = w * ri2;
-                float X = (w * g) * fmaf(K.y, g, K.x);
-                X = fmaf(3.0f, dD, X) - E.w;
-                X = fmaf(-K.w, g, X);
-                const float cR = X * ri5;
-                const float cE = fmaf(-D.w, ri2, fmaf(K.w, g, K.z) * g) * ri3;
-                qx[u] = fmaf(cR, rx, fmaf(-cE, E.x, fmaf(-ri3, D.x, qx[u])));
-                qy[u] = fmaf(cR, ry, fmaf(-cE, E.y, fmaf(-ri3, D.y, qy[u])));
-                qz[u] = fmaf(cR, rz, fmaf(-cE, E.z, fmaf(-ri3, D.z, qz[u])));
-                if (LJ && inside) {  // tabulated mean LJ force (:291-305)
-                    const float dist = __fsqrt_rn(d2);
-                    const int bin = (int)__fmaf_rn(__fsub_rn(dist, f_r0), f_inv, 0.5f);
-                    if (bin >= 0 && bin < nf) {
-                        const float2 tv = __ldg(a.ftab + frow[u] + bin);
-                        const float fr = (dist - fmaf((float)bin, f_dr, f_r0)) * f_inv;
-                        const float fv = fmaf(fr, tv.y - tv.x, tv.x) * P.w * ri;
-                        lx[u] = fmaf(fv, rx, lx[u]);
-                        ly[u] = fmaf(fv, ry, ly[u]);
-                        lz[u] = fmaf(fv, rz, lz[u]);
-                    }
-                }
+                pair(k, u, rx, ry, rz, dist2f(rx, ry, rz), std::false_type{});
             }
         }
 #pragma unroll
@@ -500,7 +537,10 @@ int force_blocks_per_sm(int atoms_per_thread) {
 
 void launch_force(const ForceArgs &a, cudaStream_t s) {
     if (a.n_items <= 0) return;
-    if (a.atoms_per_thread == 2) {
+    if (a.vote && a.atoms_per_thread != 2) {
+        if (a.terms & 2) force_kernel<true, 1, true><<<a.n_items, ForceShape<1>::kThreads, 0, s>>>(a);
+        else force_kernel<false, 1, true><<<a.n_items, ForceShape<1>::kThreads, 0, s>>>(a);
+    } else if (a.atoms_per_thread == 2) {
         if (a.terms & 2) force_kernel<true, 2><<<a.n_items, ForceShape<2>::kThreads, 0, s>>>(a);
         else force_kernel<false, 2><<<a.n_items, ForceShape<2>::kThreads, 0, s>>>(a);
     } else {

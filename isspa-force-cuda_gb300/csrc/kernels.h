@@ -47,6 +47,7 @@ struct ForceArgs {
     float f_r0, f_dr, f_inv;
     int terms;             // 1 multipole, 2 tabulated LJ, 4 CDD
     int atoms_per_thread;  // 1 (128-thread blocks) or 2 (64-thread blocks)
+    int vote;              // 1: points in warp-voted groups of four (same results)
     unsigned long long *facc;  // [Ntot][3]
     int *status;
 };

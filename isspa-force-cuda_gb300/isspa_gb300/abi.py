@@ -51,7 +51,7 @@ class EngineOptions(C.Structure):
     _fields_ = [("isspa_terms", C.c_int), ("nonbond_terms", C.c_int), ("use_graph", C.c_int),
                 ("field_split", C.c_int), ("force_chunk", C.c_int), ("mem_cap", C.c_size_t),
                 ("force_atoms_per_thread", C.c_int), ("force_tail_chunk", C.c_int),
-                ("field_vote", C.c_int)]
+                ("field_vote", C.c_int), ("force_vote", C.c_int)]
 
 
 class RunConfig(C.Structure):
@@ -76,7 +76,7 @@ class NoallocInputs(C.Structure):
 
 
 NOALLOC_SCRATCH_BYTES = 16 << 20
-SHAPE_COUNT = 10  # ISSPA_SHAPE_COUNT
+SHAPE_COUNT = 11  # ISSPA_SHAPE_COUNT
 TERMS_NONE = -1  # ISSPA_TERMS_NONE: switches the IS-SPA or nonbond pass off
 
 # isspa_energies components (the ISSPA_E_* enum), kcal/mol

@@ -24,7 +24,7 @@ class Engine:
     def __init__(self, windows: "System | Sequence[System]", isspa_terms: int = 7,
                  nonbond_terms: int = 7, use_graph: bool = True, field_split: int = 0,
                  force_chunk: int = 0, mem_cap: int = 0, force_atoms_per_thread: int = 0,
-                 force_tail_chunk: int = 0, field_vote: int = 0):
+                 force_tail_chunk: int = 0, field_vote: int = 0, force_vote: int = 0):
         if isinstance(windows, System):
             windows = [windows]
         self.windows = list(windows)
@@ -43,6 +43,7 @@ class Engine:
         opt.force_atoms_per_thread = int(force_atoms_per_thread)
         opt.force_tail_chunk = int(force_tail_chunk)
         opt.field_vote = int(field_vote)
+        opt.force_vote = int(force_vote)
         h = C.c_void_p()
         abi.check(L.isspa_engine_create(descs, len(self.windows), C.byref(opt), C.byref(h)), "engine create")
         self._h = h
@@ -56,7 +57,7 @@ class Engine:
         abi.check(abi.lib().isspa_engine_shapes(self._h, v), "shapes")
         keys = ("field_split", "field_tiles", "force_chunk", "force_items", "nonbond_items",
                 "nonbond_partners_per_item", "sms", "force_atoms_per_thread", "force_tail_chunk",
-                "field_vote")
+                "field_vote", "force_vote")
         return dict(zip(keys, list(v)))
 
     def autotune(self, reps: int = 3) -> dict:

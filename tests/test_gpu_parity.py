@@ -221,6 +221,24 @@ def test_force_kernel_atoms_per_thread_bit_identical(synth_medium, chunk, tail):
     assert np.array_equal(out[1], out[3])
 
 
+@pytest.mark.parametrize("chunk, tail", [(128, 0), (37, 0), (256, 32)])
+def test_force_vote_loop_bit_identical(synth_medium, chunk, tail):
+    """The warp-voted point loop of the force pass gives the per-pair loop's
+    forces and trajectory bit for bit (ragged chunks, partial tiles, short
+    chunks listed last)."""
+    out = []
+    for vote in (0, 1):
+        eng = ig.Engine(synth_medium, force_chunk=chunk, force_tail_chunk=tail, force_vote=vote)
+        assert eng.shapes()["force_vote"] == vote
+        eng.zero_forces()
+        eng.isspa_force()
+        out.append(eng.forces())
+        eng.step(5)
+        out.append(eng.positions())
+    assert np.array_equal(out[0], out[2])
+    assert np.array_equal(out[1], out[3])
+
+
 @pytest.mark.parametrize("chunk, tail", [(512, 32), (128, 16), (64, 0)])
 def test_force_work_list_with_short_items_last(synth_medium, chunk, tail):
     """Long chunks followed by short ones cover every (atom, point) pair once:
