@@ -277,9 +277,14 @@ def test_point_injection(adi2_100):
     assert nrel(eng.forces(), o.isspa_force(o.mc_points(seed=s.seed, step=0))) < FORCE_TOL
 
 
-def test_batched_windows_match_oracle():
+@pytest.mark.parametrize("shapes", [{}, {"force_chunk": 96, "force_tail_chunk": 32, "field_split": 4,
+                                         "field_vote": 1, "force_vote": 1}], ids=["default", "tail-vote"])
+def test_batched_windows_match_oracle(shapes):
+    """Windows of different sizes in one engine against the oracle window by
+    window, with the default shapes and with short force chunks listed last
+    (per-window tail stretches) and both warp-voted loops."""
     wins = ig.synth.config_batched(n_windows=3, seed=9)
-    eng = ig.Engine(wins)
+    eng = ig.Engine(wins, **shapes)
     f = eng.compute_forces()
     off = 0
     com, cv = eng.us_com()
