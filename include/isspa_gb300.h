@@ -252,8 +252,9 @@ int isspa_get_us_com(isspa_engine *e, double *com, double *cv);
  * pos/vel/force (float [n_atoms_total][4] each; any may be NULL).  This is
  * the call a host-side driver makes per step.  When every non-NULL buffer is a
  * 16-byte aligned range inside isspa_host_alloc memory, two small kernels move
- * the state over the host link around the step; otherwise one copy per
- * buffer.  Same results either way. */
+ * the state over the host link around the step, launched with it as one graph
+ * per set of buffers (the last four sets kept); otherwise one copy per buffer.
+ * Same results either way. */
 int isspa_step_host(isspa_engine *e, const float *pos_in, const float *vel_in, float *pos_out,
                     float *vel_out, float *force_out);
 

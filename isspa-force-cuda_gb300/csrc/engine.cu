@@ -277,6 +277,7 @@ struct isspa_engine {
         if (graph1) cudaGraphExecDestroy(graph1);
         if (graphN) cudaGraphExecDestroy(graphN);
         if (graph_timed) cudaGraphExecDestroy(graph_timed);
+        for (const HostStepGraph &h : host_graphs) cudaGraphExecDestroy(h.exec);
         for (auto ev : tev) cudaEventDestroy(ev);
         for (auto ev : kev)
             if (ev) cudaEventDestroy(ev);
@@ -505,11 +506,52 @@ struct isspa_engine {
         ck(e);
         return ex;
     }
+    // isspa_step_host with mapped buffers: copy-in kernel, step and copy-out
+    // kernel captured as one graph per set of buffer device addresses (the
+    // last few sets kept).  The addresses are resolved through the buffer
+    // registry on every call, so a graph is only launched for live buffers.
+    struct HostStepGraph {
+        const void *key[5];
+        cudaGraphExec_t exec;
+    };
+    std::vector<HostStepGraph> host_graphs;
+    cudaGraphExec_t host_step_graph(const void *const key[5], const Copy3Args &in, bool has_in, const Copy3Args &out,
+                                    bool has_out) {
+        for (const HostStepGraph &h : host_graphs)
+            if (std::equal(h.key, h.key + 5, key)) return h.exec;
+        cudaGraph_t g = nullptr;
+        ck(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        try {
+            if (has_in) launch_copy3(in, stream);
+            enqueue_step_forked();
+            if (has_out) launch_copy3(out, stream);
+        } catch (...) {
+            cudaStreamEndCapture(stream, &g);
+            if (g) cudaGraphDestroy(g);
+            throw;
+        }
+        ck(cudaStreamEndCapture(stream, &g));
+        cudaGraphExec_t ex = nullptr;
+        cudaError_t err = cudaGraphInstantiate(&ex, g, cudaGraphInstantiateFlagUseNodePriority);
+        cudaGraphDestroy(g);
+        ck(err);
+        if (host_graphs.size() >= 4) {
+            cudaGraphExecDestroy(host_graphs.front().exec);
+            host_graphs.erase(host_graphs.begin());
+        }
+        HostStepGraph h;
+        std::copy(key, key + 5, h.key);
+        h.exec = ex;
+        host_graphs.push_back(h);
+        return ex;
+    }
     void invalidate_graphs() {
         if (graph1) cudaGraphExecDestroy(graph1);
         if (graphN) cudaGraphExecDestroy(graphN);
         if (graph_timed) cudaGraphExecDestroy(graph_timed);
         graph1 = graphN = graph_timed = nullptr;
+        for (const HostStepGraph &h : host_graphs) cudaGraphExecDestroy(h.exec);
+        host_graphs.clear();
     }
     void run_steps(int nsteps) {
         if (!opt.use_graph) {
@@ -1529,12 +1571,18 @@ int isspa_step_host(isspa_engine *e, const float *pin, const float *vin, float *
     const bool direct = (!pin || dpin) && (!vin || dvin) && (!pout || dpout) && (!vout || dvout) && (!fout || dfout);
     return run_guarded([&] {
         if (direct) {
-            if (pin || vin) launch_copy3(Copy3Args{{dpin, dvin, nullptr}, {e->pos, e->vel, nullptr}, e->n_atoms}, e->stream);
-            e->run_steps(1);
-            if (pout || vout || fout)
-                launch_copy3(Copy3Args{{pout ? e->pos : nullptr, vout ? e->vel : nullptr, fout ? e->force_out : nullptr},
-                                       {dpout, dvout, dfout}, e->n_atoms},
-                             e->stream);
+            const Copy3Args in{{dpin, dvin, nullptr}, {e->pos, e->vel, nullptr}, e->n_atoms};
+            const Copy3Args out{{pout ? e->pos : nullptr, vout ? e->vel : nullptr, fout ? e->force_out : nullptr},
+                                {dpout, dvout, dfout}, e->n_atoms};
+            const bool has_in = pin || vin, has_out = pout || vout || fout;
+            if (e->opt.use_graph) {
+                const void *key[5] = {dpin, dvin, dpout, dvout, dfout};
+                ck(cudaGraphLaunch(e->host_step_graph(key, in, has_in, out, has_out), e->stream));
+            } else {
+                if (has_in) launch_copy3(in, e->stream);
+                e->run_steps(1);
+                if (has_out) launch_copy3(out, e->stream);
+            }
             ck(cudaGetLastError());
         } else {
             if (pin) ck(cudaMemcpyAsync(e->pos, pin, b, cudaMemcpyHostToDevice, e->stream));
