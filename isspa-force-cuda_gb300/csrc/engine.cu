@@ -6,7 +6,7 @@
 //   facc                  int64  [Ntot][3]     fixed-point force accumulator
 //   atype                 int2   [Ntot]        LJ type, IS-SPA type
 //   atom_win              int    [Ntot]
-//   points (SoA float4)   [Ptot] x4            per-point field-pass results
+//   points (SoA float4)   [Ptot] x5            per-point field-pass results (q0..q4)
 //   tables                g/E packed float4, force packed float2, LJ A/B float2
 // Windows are concatenated; every work list is built once at creation.
 #include <algorithm>
