@@ -119,6 +119,27 @@ __global__ void __launch_bounds__(FieldShape<S>::kThreads) field_kernel(FieldArg
     const float rm2 = __fmul_rn(rm, rm);
     const float L = W.box, h = W.hbox;
 
+    const int nb = a.n_gbins;
+    // one round of the window's atoms into shared memory: [j0, j0 + jn)
+    auto stage_round = [&](int j0, int jn) {
+        auto stage = [&](int i) {
+            const int j = W.atom_off + j0 + i;
+            float4 xj = a.pos[j];
+            xj.w = a.e0 * xj.w;  // e0*q (isspa_force_cuda.cu:179, :183)
+            s_atom[i] = xj;
+            s_row[i] = a.atype[j].y * nb;
+        };
+        if (kA == kT) {
+            if (threadIdx.x < jn) stage(threadIdx.x);
+        } else {
+#pragma unroll 1
+            for (int i = threadIdx.x; i < jn; i += kT) stage(i);
+        }
+    };
+    // the first round is staged before the points are known, so its loads
+    // overlap the draws and the barrier below covers both
+    stage_round(0, min(kA, W.n_atoms));
+
     float px, py, pz;
     if (kShareDraws) {
         // one warp of each group draws the group's 32 points (rejection
@@ -136,12 +157,15 @@ __global__ void __launch_bounds__(FieldShape<S>::kThreads) field_kernel(FieldArg
         px = s_pt[0][slot];
         py = s_pt[1][slot];
         pz = s_pt[2][slot];
-    } else if (GEN) {
-        mc_point((uint32_t)pw, (uint32_t)tile.x, *a.step_ptr, a.seed_lo, a.seed_hi, xo, rm, px, py, pz);
     } else {
-        px = a.pts_in[3 * pg + 0];
-        py = a.pts_in[3 * pg + 1];
-        pz = a.pts_in[3 * pg + 2];
+        if (GEN) {
+            mc_point((uint32_t)pw, (uint32_t)tile.x, *a.step_ptr, a.seed_lo, a.seed_hi, xo, rm, px, py, pz);
+        } else {
+            px = a.pts_in[3 * pg + 0];
+            py = a.pts_in[3 * pg + 1];
+            pz = a.pts_in[3 * pg + 2];
+        }
+        __syncthreads();  // first round staged
     }
 
     float w = 1.0f;
@@ -152,7 +176,6 @@ __global__ void __launch_bounds__(FieldShape<S>::kThreads) field_kernel(FieldArg
     // the field table shares the density bin (:170-174): interpolation across
     // that bin's edges is continuous only when both tables use one radial grid
     const bool one_grid = g_r0 == e_r0 && g_dr == e_dr;
-    const int nb = a.n_gbins;
 
     // geometry of the pair (point, staged atom k); true when inside rmax of
     // the owner's type (:154)
@@ -201,21 +224,11 @@ __global__ void __launch_bounds__(FieldShape<S>::kThreads) field_kernel(FieldArg
 
     for (int j0 = 0; j0 < W.n_atoms; j0 += kA) {
         const int jn = min(kA, W.n_atoms - j0);
-        __syncthreads();
-        auto stage = [&](int i) {
-            const int j = W.atom_off + j0 + i;
-            float4 xj = a.pos[j];
-            xj.w = a.e0 * xj.w;  // e0*q (isspa_force_cuda.cu:179, :183)
-            s_atom[i] = xj;
-            s_row[i] = a.atype[j].y * nb;
-        };
-        if (kA == kT) {
-            if (threadIdx.x < jn) stage(threadIdx.x);
-        } else {
-#pragma unroll 1
-            for (int i = threadIdx.x; i < jn; i += kT) stage(i);
+        if (j0 > 0) {
+            __syncthreads();  // the previous round has been read
+            stage_round(j0, jn);
+            __syncthreads();
         }
-        __syncthreads();
         int k = sp;
         // Groups of kG staged atoms: one warp vote tells whether any lane has
         // any of them inside rmax.  When none does, their out-of-range Coulomb
