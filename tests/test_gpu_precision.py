@@ -58,3 +58,21 @@ def test_precision_workload_against_fp64_oracle_samples(big):
     for k, v in errs.items():
         assert v < TOL, (k, v)
     assert eng.device_status() == 0
+
+
+def test_precision_workload_voted_loops_bit_identical(big):
+    """At this size almost every group of four atoms (field pass) or points
+    (force pass) is out of range for all lanes, the case the warp-voted loops
+    speed up; with the same split and chunks they reproduce the per-pair loops'
+    IS-SPA force of all 16 384 atoms bit for bit."""
+    out = []
+    for vote in (0, 1):
+        eng = ig.Engine(big, field_split=1, force_chunk=512, force_tail_chunk=64, field_vote=vote, force_vote=vote)
+        sh = eng.shapes()
+        assert sh["field_vote"] == vote and sh["force_vote"] == vote
+        eng.zero_forces()
+        eng.isspa_force()
+        out.append(eng.forces())
+        assert eng.device_status() == 0
+        eng.close()
+    assert np.array_equal(out[0], out[1])
