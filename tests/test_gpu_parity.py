@@ -278,13 +278,19 @@ def test_point_injection(adi2_100):
 
 
 @pytest.mark.parametrize("shapes", [{}, {"force_chunk": 96, "force_tail_chunk": 32, "field_split": 4,
-                                         "field_vote": 1, "force_vote": 1}], ids=["default", "tail-vote"])
+                                         "field_vote": 1, "force_vote": 1}, "autotuned"],
+                         ids=["default", "tail-vote", "autotuned"])
 def test_batched_windows_match_oracle(shapes):
     """Windows of different sizes in one engine against the oracle window by
-    window, with the default shapes and with short force chunks listed last
-    (per-window tail stretches) and both warp-voted loops."""
+    window: with the default shapes, with short force chunks listed last
+    (per-window tail stretches) and both warp-voted loops, and with whatever
+    the autotuner picks."""
     wins = ig.synth.config_batched(n_windows=3, seed=9)
-    eng = ig.Engine(wins, **shapes)
+    if shapes == "autotuned":
+        eng = ig.Engine(wins)
+        print(eng.autotune())
+    else:
+        eng = ig.Engine(wins, **shapes)
     f = eng.compute_forces()
     off = 0
     com, cv = eng.us_com()
