@@ -10,9 +10,14 @@ leapfrog (graph-replayed).
 
 The gb300 arm prints one JSON line with device-timed throughput, the end-to-end
 figure through the C ABI with host buffers, the roofline of the dominant
-kernel and the CPU oracle timed on this host as a baseline.  The reference arm
-times the CPU restatement of the reference algorithm (the reference's CUDA code
-cannot be built where this runs) with all host threads on the same workload.
+kernel and two CPU baselines timed on this host: the reference's own OpenMP
+path (src/isspa_force.omp.c, compiled unmodified) and the FP64 CPU oracle
+(same physics as the engine).  Further sections: the 44-atom system, the
+reference's published ADI2 umbrella run through the drop-in executable, 64
+umbrella windows in one engine, the 16 384-atom precision workload and the
+adjoint.  The reference arm times the reference's OpenMP path with all host
+threads on the same workload (the FP64 oracle where that file cannot be
+built).
 """
 from __future__ import annotations
 
@@ -25,7 +30,8 @@ import threading
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
-for p in (os.path.join(ROOT, "isspa-force-cuda_gb300"), os.path.join(ROOT, "oracle")):
+for p in (os.path.join(ROOT, "isspa-force-cuda_gb300"), os.path.join(ROOT, "oracle"),
+          os.path.join(ROOT, "oracle", "ref_omp")):
     if p not in sys.path:
         sys.path.insert(0, p)
 
@@ -129,28 +135,82 @@ def ncu_traffic(kernel: str):
     return d.get(kernel)
 
 
-def cpu_oracle_rate(system, budget_s: float, min_steps: int = 1, max_steps: int = 1000000, gpu_force=None):
-    """Full force evaluations + leapfrog of the oracle on all host cores.  With
-    `gpu_force` (the engine's total force of step 0 on the same state) the
-    first oracle step also checks it: normwise max |dF| / max |F|."""
+def force_errors(f, ref, floor=0.05):
+    """Normwise max |dF| / max |F| and the per-atom |dF_i| / |F_i| (median,
+    max) over atoms with |F_i| >= floor x the largest |F|."""
+    f = np.asarray(f, np.float64)[:, :3]
+    ref = np.asarray(ref, np.float64)[:, :3]
+    mag = np.linalg.norm(ref, axis=1)
+    sel = mag >= floor * mag.max()
+    rel = np.linalg.norm(f - ref, axis=1)[sel] / mag[sel]
+    return {"normwise": float(np.abs(f - ref).max() / np.abs(ref).max()),
+            "per_atom_median": float(np.median(rel)), "per_atom_max": float(rel.max()),
+            "per_atom_floor": floor, "atoms_checked": int(sel.sum())}
+
+
+def cpu_oracle_rate(system, budget_s: float, min_steps: int = 1, max_steps: int = 1000000, gpu_force=None,
+                    warmup: int = 0):
+    """Full force evaluations + leapfrog of the FP64 oracle on all host cores.
+    With `gpu_force` (the engine's total force of step 0 on the same state)
+    the first oracle step also checks it (force_errors)."""
     import oracle
 
     oracle.build()
     cores = host_cores()
     o = oracle.Oracle(system, threads=cores)
     err = None
+    for k in range(warmup):
+        o.total_force(seed=system.seed, step=k)
     t0 = time.perf_counter()
     n = 0
     while n < max_steps:
         f, _, _ = o.total_force(seed=system.seed, step=n)
         if n == 0 and gpu_force is not None:
-            err = float(np.abs(np.asarray(gpu_force)[:, :3] - f).max() / np.abs(f).max())
+            err = force_errors(gpu_force, f)
         o.leapfrog(f, seed=system.seed, step=n)
         n += 1
         if n >= min_steps and time.perf_counter() - t0 >= budget_s:
             break
     dt = time.perf_counter() - t0
     return system.n_atoms * n / dt, n, dt, cores, err
+
+
+def ref_omp():
+    """The reference's OpenMP path bound to the 1100-atom system, or the reason it is unavailable."""
+    try:
+        import isspa_gb300.synth as synth
+        from time_ref_omp import RefOmp
+
+        return RefOmp(synth.config_plain(seed=2)), None
+    except Exception as exc:  # no checkout and no staged copy, or no compiler
+        return None, f"{type(exc).__name__}: {exc}"
+
+
+def cpu_reference_omp(budget_s: float):
+    """cpu_baseline of kind "reference": the reference's own OpenMP CPU path on
+    all host cores (and on one), one call per step."""
+    from time_ref_omp import CAVEAT, cpu_model
+
+    r, why = ref_omp()
+    if r is None:
+        return None, why
+    cores = host_cores()
+    r.call(cores)  # warm-up
+    v, n, dt = r.rate(cores, budget_s, min_calls=3)
+    v1, n1, dt1 = r.rate(1, budget_s / 2, min_calls=1)
+    return {"value": round(v, 1), "unit": UNIT, "cores": cores, "kind": "reference",
+            "sample": f"{n} calls of cpu_ispa_force (src/isspa_force.omp.c:11-105, compiled unmodified) on the "
+                      f"same 1100-atom system, nMC 50, {cores} OpenMP threads ({dt:.1f} s)",
+            "one_thread": {"value": round(v1, 1), "calls": n1, "seconds": round(dt1, 2)},
+            "cpu": cpu_model(), "caveat": CAVEAT, "source_sha256": r.source_sha256}, None
+
+
+def workload_config():
+    """The workload both arms report (identical dicts)."""
+    return {"workload": "plain drop-in path: 1100 atoms (50 x 22-atom chains), nMC=50, 60 A box, "
+                        "all-pairs nonbond + IS-SPA, leapfrog/Andersen 298 K, dt 2 fs",
+            "n_atoms": 1100, "n_mc": 50, "mc_points": 55000, "box_A": 60.0,
+            "l2": "256 MB written between timed steps (outside the timed intervals)"}
 
 
 def run_gb300(args):
@@ -236,20 +296,21 @@ def run_gb300(args):
     launches = int(sum(v[1] for v in kern.values()))
 
     cpu_value, cpu_steps, cpu_s, cores, f_err = cpu_oracle_rate(sysm, budget_s=args.cpu_budget, gpu_force=f_step0)
+    port = {"value": round(cpu_value, 1), "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{cpu_steps} full MD steps of the same 1100-atom system ({cpu_s:.1f} s), FP64 CPU oracle "
+                      "(the engine's physics: bonded, IS-SPA, nonbond, leapfrog), OpenMP"}
+    ref_line, ref_why = cpu_reference_omp(budget_s=args.cpu_budget / 2)
+    cfg = workload_config()
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_step, 5), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "ns_per_day": round(ns_per_day(args.steps / (total_ms * 1e-3)), 1),
-        "config": {"workload": "plain drop-in path: 1100 atoms (50 x 22-atom chains), nMC=50, 60 A box, "
-                               "all-pairs nonbond + IS-SPA, leapfrog/Andersen 298 K, dt 2 fs",
-                   "n_atoms": N, "n_mc": M, "mc_points": P, "box_A": 60.0,
-                   "l2": "256 MB written between timed steps (outside the timed intervals)",
-                   "timing": "value: K single-step graph replays, CUDA events around each; kernel durations: "
-                             "K more replays of the step captured with events around every kernel",
-                   "instrumented_ms_per_step": round(instr_ms / args.steps, 5),
-                   "warmup_extra_steps": warm_steps,
-                   "launch_shapes": shapes, "graph": True},
+        "config": cfg,
+        "run": {"timing": "value: K single-step graph replays, CUDA events around each; kernel durations: "
+                          "K more replays of the step captured with events around every kernel",
+                "graph": True, "instrumented_ms_per_step": round(instr_ms / args.steps, 5),
+                "warmup_extra_steps": warm_steps, "launch_shapes": shapes},
         "e2e": {"value": round(e2e, 1), "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes,
                 "d2h_bytes_per_step": 3 * nbytes,
                 "path": "isspa_step_host per step (host wall clock, synchronous call) with isspa_host_alloc "
@@ -257,16 +318,20 @@ def run_gb300(args):
         "gpu_launches": launches,
         "kernel_ms_per_launch": {k: round(v, 5) for k, v in avg.items()},
         "roofline": roof,
-        "cpu_baseline": {"value": round(cpu_value, 1), "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{cpu_steps} full MD steps of the same 1100-atom system "
-                                   f"({cpu_s:.1f} s), CPU oracle (FP64 values), OpenMP"},
+        "cpu_baseline": ref_line if ref_line is not None else port,
+        "cpu_baseline_port": port,
         "device_status": status,
-        "force_error": {"normwise_vs_fp64_oracle": f_err, "target": 1e-5,
-                        "what": "total force of step 0 (bonded, IS-SPA, nonbond), same Philox MC points, "
-                                "max |F_gpu - F_oracle| / max |F_oracle|"},
+        "force_error": dict(f_err or {}, target=1e-5,
+                            what="total force of step 0 (bonded, IS-SPA, nonbond) against the FP64 oracle on the "
+                                 "same Philox MC points"),
     }
+    if ref_line is None:
+        line["cpu_baseline_reference_unavailable"] = ref_why
     clocks = clk.summary()
     line["clocks"] = clocks
+    if not args.no_extra:
+        line["small_44"] = run_small(ig, args)
+        line["adi2_published"] = run_adi2_published(args)
     if not args.no_batched:
         line["batched"] = run_batched(ig, args, value)
     if not args.no_extra:
@@ -275,30 +340,120 @@ def run_gb300(args):
     print(json.dumps(line))
 
 
+def run_small(ig, args):
+    """The 44-atom system (2 chains of 22, nMC 20, 40 A box): single-step
+    graph replays timed with events (L2 flushed between them, as the headline),
+    and a production-style run of back-to-back 8-step graphs timed on the host
+    clock, the way the reference's run logs measure ns/day."""
+    import oracle
+
+    s = ig.synth.config_small(seed=1)
+    eng = ig.Engine(s)
+    f0 = eng.compute_forces()
+    eng.zero_forces()
+    shapes = eng.autotune()
+    ref, _, _ = oracle.Oracle(s).total_force(seed=s.seed, step=0)
+    eng.step(200)
+    steps = max(200, args.steps)
+    ms = eng.time_steps(steps, L2_FLUSH)
+    _, kern = eng.time_steps_detailed(steps, L2_FLUSH)
+    n_run = 40000
+    eng.synchronize()
+    t0 = time.perf_counter()
+    eng.step(n_run)
+    eng.synchronize()
+    dt = time.perf_counter() - t0
+    status = eng.device_status()
+    eng.close()
+    return {"workload": "44 atoms (2 x 22-atom chains), nMC=20, 40 A box, leapfrog/Andersen 298 K, dt 2 fs",
+            "steps": steps, "value": round(s.n_atoms * steps / (ms * 1e-3), 1), "unit": UNIT,
+            "ms_per_step": round(ms / steps, 5), "ns_per_day": round(ns_per_day(steps / (ms * 1e-3)), 1),
+            "run": {"steps": n_run, "seconds": round(dt, 4), "value": round(s.n_atoms * n_run / dt, 1),
+                    "ns_per_day": round(ns_per_day(n_run / dt), 1),
+                    "timing": "isspa_step over back-to-back 8-step graphs, host wall clock"},
+            "kernel_ms_per_launch": {k: round(v[0] / max(v[1], 1), 5) for k, v in kern.items()},
+            "launch_shapes": shapes, "device_status": status, "force_error": force_errors(f0, ref)}
+
+
+ADI2_PUBLISHED_NS_DAY = 1272.74  # timing_tests/ADI2_US/window_10.0/ADI2.run0.log:66, GeForce GTX 1080
+
+
+def run_adi2_published(args, n_steps: int = 50000):
+    """The reference's published ADI2 umbrella run (44 atoms, nMC 100, 200 A
+    box, US k = 20 at x0 = 10 A, seed 34669, trajectory output every 1000
+    steps) through the drop-in executable on the reference's own input files,
+    with its own ns/day report (wall clock of the step loop, as the
+    reference's timing_class)."""
+    import re
+    import shutil
+    import tempfile
+
+    golden = os.path.join(ROOT, "tests", "golden")
+    exe = os.path.join(ROOT, "isspa-force-cuda_gb300", "total_force_gb300")
+    with tempfile.TemporaryDirectory() as d:
+        for f in ("ADI2.prmtop", "ADI2.isspatop", "ADI2.rst7"):
+            shutil.copy(os.path.join(golden, f), os.path.join(d, f))
+        with open(os.path.join(golden, "ADI2.us")) as f:
+            us = f.read().replace("XXX", "10.0")
+        with open(os.path.join(d, "us_params.dat"), "w") as f:
+            f.write(us)
+        cfg = "\n".join([
+            "velRst = 0", "inputVel = notread.rst", "prmtop = ADI2.prmtop", "inputCoord = ADI2.rst7",
+            "isspaPrmtop = ADI2.isspatop", "forFile = forces.xyz", "posFile = positions.xyz",
+            "velFile = velocities.xyz", "posRstFile = positions.rst", "velRstFile = velocities.rst",
+            "nMC = 100", f"nSteps = {n_steps}", "deltaWrite = 1000", "temperature = 298.00", "seed = 34669",
+            "cutoff = 12.0", "dielectric = 1.0", "boxLength = 200.0", "US = 1", "usCfgFile = us_params.dat", ""])
+        with open(os.path.join(d, "config.txt"), "w") as f:
+            f.write(cfg)
+        r = subprocess.run([exe, "config.txt"], cwd=d, capture_output=True, text=True, timeout=600)
+        if r.returncode != 0:
+            return {"error": f"drop-in executable exited {r.returncode}: {r.stderr.strip()[-300:]}"}
+        m = re.search(r"Average ns/day =\s*([0-9.]+)", r.stdout)
+        t = re.search(r"Elapsed CPU/GPU time =\s*([0-9.]+) ms", r.stdout)
+        shapes = re.search(r"launch shapes: (.*)", r.stdout)
+    nsd = float(m.group(1))
+    ms = float(t.group(1))
+    return {"workload": "ADI2 dimer (44 atoms), the reference's published umbrella run settings: nMC 100, "
+                        "200 A box, US k=20 x0=10 A, seed 34669, output every 1000 steps, no thermostat line "
+                        "(pnu 0), reference input files",
+            "steps": n_steps, "ns_per_day": nsd, "seconds": round(ms * 1e-3, 3),
+            "value": round(44 * n_steps / (ms * 1e-3), 1), "unit": UNIT,
+            "published_ns_per_day": ADI2_PUBLISHED_NS_DAY, "published_hardware": "GeForce GTX 1080",
+            "ratio_vs_published": round(nsd / ADI2_PUBLISHED_NS_DAY, 2),
+            "launch_shapes": shapes.group(1) if shapes else None,
+            "timing": "total_force_gb300 step loop, host wall clock (timing_class.cpp:57-58)"}
+
+
 def run_batched(ig, args, plain_value):
-    """64 umbrella windows (44..1100 atoms) in one engine vs the plain per-window path."""
+    """64 umbrella windows (44..1100 atoms) in one engine against the plain
+    single-window path run window by window on the same GPU (the way the
+    reference runs one window per process), both timed as single-step graph
+    replays with 256 MB written between steps."""
     wins = ig.synth.config_batched(n_windows=64, seed=4)
     eng = ig.Engine(wins)
     shapes = eng.shapes() if args.no_autotune else eng.autotune()
     nat = sum(w.n_atoms for w in wins)
-    steps = max(3, args.steps // 10)
+    steps = max(200, args.steps)
     eng.step(3)
     ms = eng.time_steps(steps, L2_FLUSH)
-    _, kern = eng.time_steps_detailed(steps, L2_FLUSH)
+    _, kern = eng.time_steps_detailed(min(steps, 50), L2_FLUSH)
+    status = eng.device_status()
     batched = nat * steps / (ms * 1e-3)
-    # plain path: each window alone in its own engine, one after another
-    plain_ms = 0.0
+    eng.close()
+    plain_ms, plain_steps = 0.0, 20
     for w in wins:
         e1 = ig.Engine(w)
         e1.step(3)
-        plain_ms += e1.time_steps(10, 0) / 10
+        plain_ms += e1.time_steps(plain_steps, L2_FLUSH) / plain_steps
         e1.close()
     plain = nat / (plain_ms * 1e-3)
-    eng.close()
-    return {"windows": len(wins), "atoms_total": nat, "steps": steps,
+    return {"windows": len(wins), "atoms_total": nat, "steps": steps, "seconds_timed": round(ms * 1e-3, 3),
             "value": round(batched, 1), "unit": UNIT, "ms_per_step": round(ms / steps, 4),
-            "plain_per_window_value": round(plain, 1), "speedup_vs_plain": round(batched / plain, 2),
-            "launch_shapes": shapes,
+            "aggregate_ns_per_day": round(len(wins) * ns_per_day(steps / (ms * 1e-3)), 1),
+            "plain_per_window_value": round(plain, 1), "plain_steps_per_window": plain_steps,
+            "speedup_vs_plain": round(batched / plain, 2),
+            "l2": "256 MB written between timed steps on both sides",
+            "launch_shapes": shapes, "device_status": status,
             "kernel_ms_per_step": {k: round(v[0] / max(v[1], 1), 4) for k, v in kern.items()}}
 
 
@@ -351,22 +506,42 @@ def run_adjoint(ig):
 
 
 def run_reference(args):
-    """CPU restatement of the reference path, all host threads, same workload."""
+    """The reference's own CPU path on all host threads: cpu_ispa_force of
+    src/isspa_force.omp.c (compiled unmodified) on the 1100-atom system, one
+    call per step, W untimed and K timed calls.  Where that file cannot be
+    built, the FP64 CPU oracle (a restatement of the reference's CUDA kernels)
+    takes its place."""
     import isspa_gb300.synth as synth
 
-    sysm = synth.config_plain(seed=2)
-    budget = args.cpu_budget * 3
-    value, n, dt, cores, _ = cpu_oracle_rate(sysm, budget_s=budget, min_steps=1,
-                                          max_steps=max(1, args.steps + args.warmup))
+    cores = host_cores()
+    r, why = ref_omp()
+    if r is not None:
+        from time_ref_omp import CAVEAT, cpu_model
+
+        for _ in range(args.warmup):
+            r.call(cores)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            r.call(cores)
+        dt = time.perf_counter() - t0
+        value = r.n * args.steps / dt
+        base = {"value": round(value, 1), "unit": UNIT, "cores": cores, "kind": "reference",
+                "sample": f"{args.steps} calls of cpu_ispa_force (src/isspa_force.omp.c:11-105, compiled "
+                          f"unmodified), 1100 atoms, nMC 50, {cores} OpenMP threads ({dt:.2f} s)",
+                "cpu": cpu_model(), "caveat": CAVEAT, "source_sha256": r.source_sha256}
+        dtype = "f32"
+    else:
+        sysm = synth.config_plain(seed=2)
+        value, n, dt, cores, _ = cpu_oracle_rate(sysm, budget_s=1e9, min_steps=args.steps, max_steps=args.steps,
+                                                 warmup=args.warmup)
+        base = {"value": round(value, 1), "unit": UNIT, "cores": cores, "kind": "port",
+                "sample": f"{n} full MD steps ({dt:.1f} s) of the FP64 CPU oracle; the reference's OpenMP file "
+                          f"is unavailable here ({why})"}
+        dtype = "f64"
     line = {"impl": "reference", "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": 1,
-            "steps": n, "warmup": 0, "ms_per_step": round(dt / n * 1e3, 3), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "plain drop-in path: 1100 atoms (50 x 22-atom chains), nMC=50, 60 A box",
-                       "n_atoms": sysm.n_atoms, "n_mc": sysm.n_mc},
-            "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"{n} full MD steps ({dt:.1f} s) of the CPU restatement of the "
-                                       "reference kernels; the reference CUDA build needs its source "
-                                       "tree, which is not present here"},
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic",
+            "config": workload_config(), "cpu_baseline": base,
             "e2e": {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 

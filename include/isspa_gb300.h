@@ -119,6 +119,11 @@ typedef struct isspa_engine_options {
     int force_vote;      /* 1: the force pass (one atom per thread) takes its points in
                             groups of four with one warp vote per group (same results);
                             0 => per-pair branches */
+    int integrator;      /* step integrator of isspa_step: 1 = bonded, umbrella and leapfrog
+                            kernels (bonded and umbrella concurrent with the IS-SPA pass);
+                            2 = one fused cooperative kernel for bonded, umbrella and
+                            leapfrog after the force passes (same results bit for bit);
+                            0 => 1 until isspa_autotune times both and keeps the faster */
 } isspa_engine_options;
 
 #define ISSPA_TERMS_NONE (-1)
@@ -181,8 +186,9 @@ int isspa_engine_info(const isspa_engine *e, int *n_windows, int *n_atoms_total,
  * item, [6] SM count used for the choice, [7] receiving atoms per force
  * thread, [8] points per force work item of the short items listed last (0:
  * none), [9] 1 when the field pass walks its atoms in warp-voted groups,
- * [10] 1 when the force pass takes its points in warp-voted groups. */
-#define ISSPA_SHAPE_COUNT 11
+ * [10] 1 when the force pass takes its points in warp-voted groups, [11] the
+ * step integrator (1 separate kernels, 2 fused; see isspa_engine_options). */
+#define ISSPA_SHAPE_COUNT 12
 int isspa_engine_shapes(const isspa_engine *e, int shape[ISSPA_SHAPE_COUNT]);
 /* Autotuner: times every field-pass atom split (per-pair and warp-voted
  * loops) and, for 1 and 2 receiving
@@ -191,7 +197,10 @@ int isspa_engine_shapes(const isspa_engine *e, int shape[ISSPA_SHAPE_COUNT]);
  * followed by about two waves of short ones; then the voted force loop on the
  * chosen list) on this engine's own
  * workload with CUDA events (reps launches each), keeps the fastest of each
- * and reports the result as isspa_engine_shapes does.  Clears the force
+ * and reports the result as isspa_engine_shapes does.  When the options leave
+ * the integrator open (0), it then times single-step graph replays with the
+ * separate and the fused integrator and keeps the faster; positions,
+ * velocities and the step counter are restored.  Clears the force
  * accumulator; invalidates captured graphs. */
 int isspa_autotune(isspa_engine *e, int reps, int shape[ISSPA_SHAPE_COUNT]);
 
@@ -202,7 +211,7 @@ int isspa_autotune(isspa_engine *e, int reps, int shape[ISSPA_SHAPE_COUNT]);
  * is only enqueued on the engine stream. */
 int isspa_zero_forces(isspa_engine *e);                   /* cudaMemset(for_d), total_force_cuda.cpp:109 */
 int bond_force_cuda(isspa_engine *e, float *ms_out);      /* bond_force_cuda.cu:58-79 */
-int angle_force_cuda(isspa_engine *e, float *ms_out);     /* angle_force_cuda.cu:158-175 */
+int angle_force_cuda(isspa_engine *e, float *ms_out);     /* angle_force_cuda.cu:69-86 */
 int dih_force_cuda(isspa_engine *e, float *ms_out);       /* dih_force_cuda.cu:140-157 */
 int isspa_force_cuda(isspa_engine *e, float *ms_out);     /* isspa_force_cuda.cu:331-360 */
 int nonbond_force_cuda(isspa_engine *e, float *ms_out);   /* nonbond_force_cuda.cu:178-194 */
@@ -221,7 +230,7 @@ int isspa_time_steps(isspa_engine *e, int nsteps, size_t flush_bytes, double *ms
  * ms_kernels[ISSPA_K_COUNT] receives the summed milliseconds per kernel and
  * launches[ISSPA_K_COUNT] the number of launches of each. */
 enum { ISSPA_K_FIELD = 0, ISSPA_K_FORCE, ISSPA_K_NONBOND, ISSPA_K_BONDED, ISSPA_K_UMBRELLA,
-       ISSPA_K_LEAPFROG, ISSPA_K_COUNT };
+       ISSPA_K_LEAPFROG, ISSPA_K_INTEGRATOR, ISSPA_K_COUNT };
 int isspa_time_steps_detailed(isspa_engine *e, int nsteps, size_t flush_bytes, double *ms_total,
                               double *ms_kernels, int *launches);
 /* Page-locked host buffers, mapped into the device address space
@@ -234,6 +243,12 @@ void isspa_host_free(void *p);
 int isspa_synchronize(isspa_engine *e);
 /* Sticky device status word (0 if nothing tripped); clears it when reset != 0. */
 int isspa_device_status(isspa_engine *e, int reset);
+/* Failure-detection testing (no counterpart in the reference): leaves the
+ * fused integrator's grid barrier as if a block had been lost mid-count, so the
+ * next fused step's bounded waits run out; that step integrates nothing and
+ * reports ISSPA_ERR_TIMEOUT through isspa_device_status, whose reset also
+ * restores the barrier.  No kernel faults and the context stays usable. */
+int isspa_debug_stall_barrier(isspa_engine *e);
 
 /* ---- state transfer (host <-> device, synchronous) ----------------------- */
 int isspa_set_positions(isspa_engine *e, const float *pos4, int n_atoms_total);
@@ -343,18 +358,28 @@ int isspa_measure_fp32_peak(double *tflops);
  * (or any allocating routine): code running inside another framework's memory
  * pool, a host process whose device memory is budgeted up front, or a real-time
  * loop that may not take the allocator's locks.  All arrays below are DEVICE
- * pointers owned by the caller; the per-point field records, packed tables and
- * force accumulator live in one static device buffer of
- * ISSPA_NOALLOC_SCRATCH_BYTES that every GPU loading this library holds until
- * the process exits.  Systems whose working set does not fit are rejected with
- * ISSPA_ERR_UNSUPPORTED (roughly 190 k MC points, e.g. 3800 atoms at nMC 50).
- * The first call on a device looks up that buffer's device address (make it
- * before any stream capture); calls share the buffer, so calls that overlap on
- * the GPU (different streams, devices' own queues) race and must be ordered by
- * the caller.  Computes the same IS-SPA force as isspa_force_cuda for one
- * window and writes it to force_out ([n_atoms][4], .w = 0), on `stream`
- * (a cudaStream_t; NULL = legacy default stream), without synchronising. */
+ * pointers owned by the caller; the work lists, per-point field records, packed
+ * tables, force accumulator and status word live in one static device buffer
+ * of ISSPA_NOALLOC_SCRATCH_BYTES that every GPU loading this library holds
+ * until the process exits.  The buffer needs 80 bytes per MC point, 32 per atom
+ * and the work lists (16 bytes per 32-128 points and per force work item);
+ * systems that do not fit are rejected with ISSPA_ERR_UNSUPPORTED before
+ * anything is enqueued (roughly 200 k MC points, e.g. 3900 atoms at nMC 50).
+ * The first call on a device looks up that buffer's device address; make that
+ * first call before any stream capture.  Calls share the buffer, so calls
+ * that overlap on the GPU (different streams) race and must be ordered by the
+ * caller.  Computes the same IS-SPA force as isspa_force_cuda for one window and
+ * writes it to force_out ([n_atoms][4], .w = 0), on `stream` (a cudaStream_t;
+ * NULL = legacy default stream), without synchronising and without any
+ * host-to-device copy.  The return value reports argument and launch errors;
+ * what the kernels find (a force beyond the fixed-point range, a non-finite
+ * force, an IS-SPA type outside [0, n_isspa_types), which is then read as type
+ * 0) is written as ISSPA_NOALLOC_STATUS_* bits to *status_out when that pointer
+ * is given, ordered after force_out on the same stream. */
 #define ISSPA_NOALLOC_SCRATCH_BYTES (16u << 20)
+#define ISSPA_NOALLOC_STATUS_OVERFLOW 1   /* a force beyond the fixed-point accumulator's range */
+#define ISSPA_NOALLOC_STATUS_NONFINITE 2  /* a non-finite force */
+#define ISSPA_NOALLOC_STATUS_BOUNDS 4     /* an index out of range (IS-SPA type) */
 typedef struct isspa_noalloc_inputs {
     int n_atoms, n_mc, n_isspa_types;
     const float *pos;         /* [n_atoms][4]: x, y, z, charge/sqrt(eps) */
@@ -366,7 +391,10 @@ typedef struct isspa_noalloc_inputs {
     float box;
     uint64_t seed;
     uint32_t step;            /* Philox step key of the MC points */
-    int terms;                /* 1 multipole, 2 tabulated LJ, 4 CDD; 0 => all */
+    int terms;                /* 1 multipole, 2 tabulated LJ, 4 CDD, any sum of them; 0 => all;
+                                 other values => ISSPA_ERR_ARG */
+    int *status_out;          /* optional device-accessible int (device or mapped host memory):
+                                 receives this call's ISSPA_NOALLOC_STATUS_* bits, 0 = clean */
 } isspa_noalloc_inputs;
 int isspa_force_noalloc(const isspa_noalloc_inputs *in, float *force_out, void *stream);
 

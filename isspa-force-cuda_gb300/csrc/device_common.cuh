@@ -25,6 +25,7 @@ enum : int {
     kStatusOverflow = 1,
     kStatusNonFinite = 2,
     kStatusBounds = 4,
+    kStatusTimeout = 8,  // a bounded device wait gave up
 };
 
 // One window (umbrella window or replica) of a batch.

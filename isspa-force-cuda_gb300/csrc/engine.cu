@@ -92,6 +92,13 @@ struct isspa_engine {
     int field_vote = 0;  // field pass in warp-voted groups of four atoms
     int force_vote = 0;  // force pass in warp-voted groups of four points (1 atom per thread)
     int force_apt = 1;  // receiving atoms per force-kernel thread (1 or 2)
+    // step integrator: 1 = bonded, umbrella and leapfrog kernels (bonded and
+    // umbrella on the forked branch), 2 = one fused cooperative kernel
+    int integrator = 1;
+    int integ_grid = 0;
+    int *bias_start = nullptr, *bias_by_atom = nullptr;
+    double2 *usf = nullptr;
+    unsigned int *bar = nullptr;
     int4 *nb_items = nullptr;
     int *nb_nj = nullptr;
     int n_nb_items = 0, nb_chunk = 0, n_sms = 0;
@@ -430,6 +437,26 @@ struct isspa_engine {
         return a;
     }
 
+    IntegratorArgs integrator_args() const {
+        IntegratorArgs a{};
+        a.bonded = bonded_args(1, 1, 1);
+        a.us = umbrella_args();
+        a.lf = leapfrog_args();
+        a.bias_start = bias_start;
+        a.bias_by_atom = bias_by_atom;
+        a.usf = usf;
+        a.bar = bar;
+        return a;
+    }
+    // Grid of the fused integrator: enough 256-thread blocks for the bonded
+    // terms, the atoms and the restrained windows, within the co-resident limit.
+    int integrator_grid() const {
+        const long long t = integrator_block_threads();
+        const long long terms = (long long)n_bonds + n_angles + n_dihs;
+        long long g = std::max<long long>({(terms + t - 1) / t, (n_atoms + t - 1) / t, (long long)n_us, 1});
+        return (int)std::min<long long>(g, std::max(1, integrator_max_blocks()));
+    }
+
     // ---------------------------------------------------------- sequences
     void enqueue_isspa(cudaStream_t s, bool raw = false) {
         launch_field(field_args(), field_split, raw, s);
@@ -448,9 +475,10 @@ struct isspa_engine {
             case ISSPA_K_FIELD: return opt.isspa_terms && n_field_tiles > 0;
             case ISSPA_K_FORCE: return opt.isspa_terms && n_force_items > 0;
             case ISSPA_K_NONBOND: return opt.nonbond_terms && n_nb_items > 0;
-            case ISSPA_K_BONDED: return n_bonds + n_angles + n_dihs > 0;
-            case ISSPA_K_UMBRELLA: return n_us > 0;
-            case ISSPA_K_LEAPFROG: return n_atoms > 0;
+            case ISSPA_K_BONDED: return integrator == 1 && n_bonds + n_angles + n_dihs > 0;
+            case ISSPA_K_UMBRELLA: return integrator == 1 && n_us > 0;
+            case ISSPA_K_LEAPFROG: return integrator == 1 && n_atoms > 0;
+            case ISSPA_K_INTEGRATOR: return integrator == 2 && n_atoms > 0;
         }
         return false;
     }
@@ -471,20 +499,28 @@ struct isspa_engine {
         mark(ISSPA_K_FORCE, 0, stream);
         launch_force(force_args(), stream);
         mark(ISSPA_K_FORCE, 1, stream);
-        mark(ISSPA_K_BONDED, 0, side);
-        launch_bonded(bonded_args(1, 1, 1), side);
-        mark(ISSPA_K_BONDED, 1, side);
-        mark(ISSPA_K_UMBRELLA, 0, side);
-        launch_umbrella(umbrella_args(), side);
-        mark(ISSPA_K_UMBRELLA, 1, side);
+        if (integrator == 1) {
+            mark(ISSPA_K_BONDED, 0, side);
+            launch_bonded(bonded_args(1, 1, 1), side);
+            mark(ISSPA_K_BONDED, 1, side);
+            mark(ISSPA_K_UMBRELLA, 0, side);
+            launch_umbrella(umbrella_args(), side);
+            mark(ISSPA_K_UMBRELLA, 1, side);
+        }
         mark(ISSPA_K_NONBOND, 0, side);
         launch_nonbond(nonbond_args(), side);
         mark(ISSPA_K_NONBOND, 1, side);
         ck(cudaEventRecord(ev_join, side));
         ck(cudaStreamWaitEvent(stream, ev_join, 0));
-        mark(ISSPA_K_LEAPFROG, 0, stream);
-        launch_leapfrog(leapfrog_args(), stream);
-        mark(ISSPA_K_LEAPFROG, 1, stream);
+        if (integrator == 2) {
+            mark(ISSPA_K_INTEGRATOR, 0, stream);
+            if (n_atoms > 0) ck(launch_integrator(integrator_args(), integ_grid, stream));
+            mark(ISSPA_K_INTEGRATOR, 1, stream);
+        } else {
+            mark(ISSPA_K_LEAPFROG, 0, stream);
+            launch_leapfrog(leapfrog_args(), stream);
+            mark(ISSPA_K_LEAPFROG, 1, stream);
+        }
     }
     cudaEvent_t kev[2 * ISSPA_K_COUNT] = {};
     cudaGraphExec_t graph_timed = nullptr;
@@ -849,6 +885,21 @@ void build(isspa_engine &E, const std::vector<isspa_host_system> &ws) {
     E.pts.q2 = E.alloc<float4>(E.n_points);
     E.pts.q3 = E.alloc<float4>(E.n_points);
     E.pts.q4 = E.alloc<float4>(E.n_points);
+    // restraint entries grouped by atom, for the fused integrator
+    {
+        std::vector<int> start(E.n_atoms + 1, 0), by_atom(bias.size());
+        for (const int2 &b : bias) ++start[b.x + 1];
+        for (int i = 0; i < E.n_atoms; ++i) start[i + 1] += start[i];
+        std::vector<int> fill(start.begin(), start.end() - 1);
+        for (size_t b = 0; b < bias.size(); ++b) by_atom[fill[bias[b].x]++] = (int)b;
+        E.bias_start = E.upload(start);
+        E.bias_by_atom = E.upload(by_atom);
+    }
+    E.usf = E.alloc<double2>(2 * (size_t)W);
+    E.bar = E.alloc<unsigned int>(2);
+    ck(cudaMemset(E.bar, 0, 2 * sizeof(unsigned int)));
+    E.integrator = E.opt.integrator == 2 ? 2 : 1;
+    E.integ_grid = E.integrator_grid();
     E.status = E.alloc<int>(1);
     E.d_step = E.alloc<uint32_t>(1);
     E.d_done = E.alloc<unsigned int>(1);
@@ -1007,6 +1058,7 @@ int isspa_engine_shapes(const isspa_engine *e, int shape[ISSPA_SHAPE_COUNT]) {
     shape[8] = e->force_tail;
     shape[9] = e->field_vote;
     shape[10] = e->force_apt == 1 ? e->force_vote : 0;
+    shape[11] = e->integrator;
     return ISSPA_OK;
 }
 
@@ -1322,7 +1374,37 @@ int isspa_autotune(isspa_engine *e, int reps, int shape[ISSPA_SHAPE_COUNT]) {
             const float voted = time_it([&] { launch_force(e->force_args(), e->stream); });
             e->force_vote = voted < plain ? 1 : 0;
         }
+        // step integrator (unless fixed by the options): the separate bonded,
+        // umbrella and leapfrog kernels against the fused cooperative kernel,
+        // timed as single-step graph replays; positions, velocities and the
+        // step counter are restored afterwards
         ck(cudaMemsetAsync(e->facc, 0, 3 * sizeof(unsigned long long) * e->n_atoms, e->stream));
+        if (e->opt.integrator == 0 && e->n_atoms > 0) {
+            std::vector<float4> p0(e->n_atoms), v0(e->n_atoms);
+            uint32_t st0 = 0;
+            ck(cudaMemcpyAsync(p0.data(), e->pos, sizeof(float4) * e->n_atoms, cudaMemcpyDeviceToHost, e->stream));
+            ck(cudaMemcpyAsync(v0.data(), e->vel, sizeof(float4) * e->n_atoms, cudaMemcpyDeviceToHost, e->stream));
+            ck(cudaMemcpyAsync(&st0, e->d_step, sizeof(uint32_t), cudaMemcpyDeviceToHost, e->stream));
+            ck(cudaStreamSynchronize(e->stream));
+            float t[3] = {0.f, 0.f, 0.f};
+            for (int m : {1, 2}) {
+                e->integrator = m;
+                e->invalidate_graphs();
+                cudaGraphExec_t g = e->capture(1);
+                auto one = [&] { ck(cudaGraphLaunch(g, e->stream)); };
+                const float first = time_it(one);
+                const int saved = reps;
+                reps = first > 2.0f ? saved : std::max(saved, 20);
+                t[m] = time_it(one);
+                reps = saved;
+                cudaGraphExecDestroy(g);
+            }
+            e->integrator = t[2] < t[1] ? 2 : 1;
+            ck(cudaMemcpyAsync(e->pos, p0.data(), sizeof(float4) * e->n_atoms, cudaMemcpyHostToDevice, e->stream));
+            ck(cudaMemcpyAsync(e->vel, v0.data(), sizeof(float4) * e->n_atoms, cudaMemcpyHostToDevice, e->stream));
+            ck(cudaMemcpyAsync(e->d_step, &st0, sizeof(uint32_t), cudaMemcpyHostToDevice, e->stream));
+            ck(cudaMemsetAsync(e->facc, 0, 3 * sizeof(unsigned long long) * e->n_atoms, e->stream));
+        }
         ck(cudaStreamSynchronize(e->stream));
         e->invalidate_graphs();
     });
@@ -1490,15 +1572,33 @@ int isspa_device_status(isspa_engine *e, int reset) {
     int st = 0;
     if (cudaStreamSynchronize(e->stream) != cudaSuccess ||
         cudaMemcpyAsync(&st, e->status, sizeof(int), cudaMemcpyDeviceToHost, e->stream) != cudaSuccess ||
-        (reset && cudaMemsetAsync(e->status, 0, sizeof(int), e->stream) != cudaSuccess) ||
         cudaStreamSynchronize(e->stream) != cudaSuccess) {
         cudaGetLastError();
         return ISSPA_ERR_CUDA;
     }
+    // a grid barrier that gave up leaves its words mid-count: reset them with the status
+    if (reset && (cudaMemsetAsync(e->status, 0, sizeof(int), e->stream) != cudaSuccess ||
+                  ((st & kStatusTimeout) && cudaMemsetAsync(e->bar, 0, 2 * sizeof(unsigned int), e->stream) != cudaSuccess) ||
+                  cudaStreamSynchronize(e->stream) != cudaSuccess)) {
+        cudaGetLastError();
+        return ISSPA_ERR_CUDA;
+    }
+    if (st & kStatusTimeout) return ISSPA_ERR_TIMEOUT;
     if (st & kStatusNonFinite) return ISSPA_ERR_NONFINITE;
     if (st & kStatusOverflow) return ISSPA_ERR_OVERFLOW;
     if (st & kStatusBounds) return ISSPA_ERR_BOUNDS;
     return ISSPA_OK;
+}
+
+int isspa_debug_stall_barrier(isspa_engine *e) {
+    int rc = guard(e);
+    if (rc) return rc;
+    return run_guarded([&] {
+        // an arrival count no grid reaches: every block waits out its limit
+        const unsigned int words[2] = {0x80000000u, 0u};
+        ck(cudaMemcpyAsync(e->bar, words, sizeof words, cudaMemcpyHostToDevice, e->stream));
+        ck(cudaStreamSynchronize(e->stream));
+    });
 }
 
 static int copy_state(isspa_engine *e, void *dst, const void *src, size_t bytes, cudaMemcpyKind k) {

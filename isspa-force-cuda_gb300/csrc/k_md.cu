@@ -111,58 +111,83 @@ __global__ void __launch_bounds__(kNbThreads) nonbond_kernel(NonbondArgs a) {
     atomicAdd(acc + 2, (unsigned long long)fza);
 }
 
-// Image vector in float (the reference's minimum-image decision), then the
-// bonded arithmetic in FP64: these terms are O(N) work, and acos / 1/sin(phi)
-// / 1/|r12 x r23| make the FP32 formulas ill-conditioned for near-planar or
-// near-linear geometries.
-__device__ __forceinline__ double3 rvec(const float4 *pos, int p, int q, float L, float h) {
+// Bonded terms in FP32.  Image vectors as the reference decides them
+// (min_image), then formulations that stay well conditioned where the
+// reference's closed forms cancel:
+//   * bond:     f = 2k (r0 - |r|) / |r| r, the difference taken before the
+//               division (bond_force_cuda.cu:36-50 writes 2k (r0/|r| - 1));
+//   * angle:    theta = atan2(|r1 x r2|, -r1.r2) and the force directions as
+//               triple products, r1 x (r1 x r2) / c11 = (c12/c11) r1 - r2 and
+//               r2 x (r1 x r2) / c22 = r1 - (c12/c22) r2, over |r1 x r2| =
+//               sqrt(c11 c22 - c12^2) (angle_force_cuda.cu:19-52);
+//   * dihedral: the torsion gradient of Blondel & Karplus, J. Comput. Chem. 17
+//               (1996) 1132, with phi = atan2 of the cross-product sine and
+//               cosine: no acos and no 1/sin(phi), so near-planar torsions keep
+//               FP32 accuracy.  The reference's energy is V (1 + cos(n phi_u -
+//               phase)) with the unsigned angle phi_u = acos(cos phi) in [0, pi]
+//               (dih_force_cuda.cu:86-135), so dU/dphi = -V n sin(n |phi| -
+//               phase) sgn(phi); an exactly planar torsion gets no force, as
+//               the reference's |cos phi| >= 1 branch.
+// Every term adds its forces through to_fix into the int64 accumulator, so
+// the result does not depend on the order of the atomics and the fused
+// integrator (which runs the same term functions) reproduces it bit for bit.
+struct F3 {
+    float x, y, z;
+};
+__device__ __forceinline__ F3 rvec(const float4 *pos, int p, int q, float L, float h) {
     const float4 a = pos[p], b = pos[q];
-    return make_double3(mimg(a.x - b.x, L, h), mimg(a.y - b.y, L, h), mimg(a.z - b.z, L, h));
+    return F3{mimg(a.x - b.x, L, h), mimg(a.y - b.y, L, h), mimg(a.z - b.z, L, h)};
 }
-
-__device__ __forceinline__ void add_force(unsigned long long *facc, int *status, int atom, double fx,
-                                          double fy, double fz) {
-    const double m = fmax(fabs(fx), fmax(fabs(fy), fabs(fz)));
-    if (!(m <= (double)kFixLimit)) atomicOr(status, (m != m || isinf(m)) ? kStatusNonFinite : kStatusOverflow);
-    unsigned long long *acc = facc + 3 * (long long)atom;
-    atomicAdd(acc + 0, (unsigned long long)__double2ll_rn(fx * 4294967296.0));
-    atomicAdd(acc + 1, (unsigned long long)__double2ll_rn(fy * 4294967296.0));
-    atomicAdd(acc + 2, (unsigned long long)__double2ll_rn(fz * 4294967296.0));
+__device__ __forceinline__ float dotf(F3 a, F3 b) { return fmaf(a.x, b.x, fmaf(a.y, b.y, a.z * b.z)); }
+__device__ __forceinline__ F3 crossf(F3 a, F3 b) {
+    return F3{fmaf(a.y, b.z, -a.z * b.y), fmaf(a.z, b.x, -a.x * b.z), fmaf(a.x, b.y, -a.y * b.x)};
 }
+__device__ __forceinline__ F3 scalef(float s, F3 a) { return F3{s * a.x, s * a.y, s * a.z}; }
 
-__device__ __forceinline__ double dot3(double3 a, double3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+// Fixed-point scatter of one atom's share of a term.
+struct FixAdd {
+    unsigned long long *facc;
+    int *status;
+    __device__ __forceinline__ void operator()(int atom, F3 f) const {
+        check_force(status, f.x, f.y, f.z);
+        fix_add3(facc + 3 * (long long)atom, f.x, f.y, f.z);
+    }
+};
 
-__global__ void bonded_kernel(BondedArgs a) {
-    long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+// Term idx of the concatenated (enabled) bond, angle and dihedral lists.
+template <class Add>
+__device__ __forceinline__ void bonded_term(const BondedArgs &a, long long idx, const Add &add) {
     const long long nb = a.do_bonds ? a.n_bonds : 0;
     const long long na = a.do_angles ? a.n_angles : 0;
     const long long nd = a.do_dihs ? a.n_dihs : 0;
-    if (idx < nb) {  // bond_force_cuda.cu:36-50: f = 2k (r0/|r| - 1) r on atom x
+    if (idx < nb) {  // bond_force_cuda.cu:36-50
         const int4 b = a.bonds[idx];
         const WinDev W = a.win[a.atom_win[b.x]];
-        const double3 r = rvec(a.pos, b.x, b.y, W.box, W.hbox);
+        const F3 r = rvec(a.pos, b.x, b.y, W.box, W.hbox);
         const float2 p = a.bond_par[b.z];
-        const double f = (double)p.x * ((double)p.y / sqrt(dot3(r, r)) - 1.0);
-        add_force(a.facc, a.status, b.x, f * r.x, f * r.y, f * r.z);
-        add_force(a.facc, a.status, b.y, -f * r.x, -f * r.y, -f * r.z);
+        const float d = __fsqrt_rn(dotf(r, r));
+        const float f = __fdiv_rn(p.x * (p.y - d), d);
+        add(b.x, scalef(f, r));
+        add(b.y, scalef(-f, r));
         return;
     }
     idx -= nb;
     if (idx < na) {  // angle_force_cuda.cu:19-52
         const int4 g = a.angles[idx];
         const WinDev W = a.win[a.atom_win[g.x]];
-        const double3 r1 = rvec(a.pos, g.x, g.y, W.box, W.hbox);
-        const double3 r2 = rvec(a.pos, g.y, g.z, W.box, W.hbox);
-        const double c11 = dot3(r1, r1), c22 = dot3(r2, r2), c12 = dot3(r1, r2);
-        const double b = -c12 / sqrt(c11 * c22);
-        const double theta = b >= 1.0 ? 1.0e-16 : (b <= -1.0 ? (double)kPi : acos(b));
+        const F3 r1 = rvec(a.pos, g.x, g.y, W.box, W.hbox);
+        const F3 r2 = rvec(a.pos, g.y, g.z, W.box, W.hbox);
+        const F3 w = crossf(r1, r2);
+        const float s = __fsqrt_rn(dotf(w, w));
+        if (!(s > 0.0f)) return;  // collinear: the reference's 1/0
+        const float theta = atan2f(s, -dotf(r1, r2));
         const float2 p = a.angle_par[g.w];
-        const double f = (double)p.x * (theta - (double)p.y) / sqrt(c11 * c22 - c12 * c12);
-        const double a1 = c12 / c11, a2 = c12 / c22;
-        add_force(a.facc, a.status, g.x, f * (a1 * r1.x - r2.x), f * (a1 * r1.y - r2.y), f * (a1 * r1.z - r2.z));
-        add_force(a.facc, a.status, g.y, f * ((1.0 + a2) * r2.x - (1.0 + a1) * r1.x),
-                  f * ((1.0 + a2) * r2.y - (1.0 + a1) * r1.y), f * ((1.0 + a2) * r2.z - (1.0 + a1) * r1.z));
-        add_force(a.facc, a.status, g.z, f * (r1.x - a2 * r2.x), f * (r1.y - a2 * r2.y), f * (r1.z - a2 * r2.z));
+        const float f = __fdiv_rn(p.x * (theta - p.y), s);
+        const F3 fi = scalef(__fdiv_rn(f, dotf(r1, r1)), crossf(r1, w));
+        const F3 fk = scalef(__fdiv_rn(f, dotf(r2, r2)), crossf(r2, w));
+        add(g.x, fi);
+        add(g.y, F3{-(fi.x + fk.x), -(fi.y + fk.y), -(fi.z + fk.z)});
+        add(g.z, fk);
         return;
     }
     idx -= na;
@@ -175,60 +200,64 @@ __global__ void bonded_kernel(BondedArgs a) {
         if (raw & 0x40000000) {  // scaled 1-4 when atoms.z > 0 && atoms.w > 0 (:60-82)
             const float2 ab = __ldg(a.ljab + a.atype[d.x].x * a.n_lj_types + a.atype[d.w].x);
             const float2 sc = a.sc14[ty];
-            const double3 r14 = rvec(a.pos, d.x, d.w, L, h);
-            const double rm = dot3(r14, r14);
-            const double r6 = 1.0 / (rm * rm * rm);
-            const double fe = (double)a.pos[d.x].w * (double)a.pos[d.w].w / (rm * sqrt(rm) * (double)sc.x);
-            const double fv = r6 * (12.0 * (double)ab.x * r6 - 6.0 * (double)ab.y) / ((double)sc.y * rm);
-            const double f = fe + fv;
-            add_force(a.facc, a.status, d.x, f * r14.x, f * r14.y, f * r14.z);
-            add_force(a.facc, a.status, d.w, -f * r14.x, -f * r14.y, -f * r14.z);
+            const F3 r14 = rvec(a.pos, d.x, d.w, L, h);
+            const float rm = dotf(r14, r14);
+            const float ri2 = __frcp_rn(rm);
+            const float r6 = ri2 * ri2 * ri2;
+            const float fe = __fdiv_rn(a.pos[d.x].w * a.pos[d.w].w, rm * __fsqrt_rn(rm) * sc.x);
+            const float fv = __fdiv_rn(r6 * fmaf(12.0f * ab.x, r6, -6.0f * ab.y) * ri2, sc.y);
+            const float f = fe + fv;
+            add(d.x, scalef(f, r14));
+            add(d.w, scalef(-f, r14));
         }
-        const double3 r12 = rvec(a.pos, d.x, d.y, L, h);
-        const double3 r23 = rvec(a.pos, d.y, d.z, L, h);
-        const double3 r34 = rvec(a.pos, d.z, d.w, L, h);
-        const double c11 = dot3(r12, r12), c22 = dot3(r23, r23), c12 = dot3(r12, r23);
-        const double c33 = dot3(r34, r34), c23 = dot3(r23, r34), c13 = dot3(r12, r34);
-        const double t1 = c13 * c22 - c12 * c23;
-        const double t2 = c11 * c23 - c12 * c13;
-        const double t3 = c12 * c12 - c11 * c22;
-        const double t4 = c22 * c33 - c23 * c23;
-        const double t5 = c13 * c23 - c12 * c33;
-        const double t6 = -t1;
-        const double b = sqrt(-t3 * t4);
-        const double cs = t6 / b;
-        double fd = 0.0;
-        if (cs > -1.0 && cs < 1.0) {
-            const double phi = acos(cs);
-            const float4 p = a.dih_par[ty];
-            fd = (double)p.x * (double)p.y * sin((double)p.x * phi - (double)p.z) * c22 / (sin(phi) * b);
-        }
-        const double g1 = fd / t3, g4 = -fd / t4;
-        const double f1x = g1 * (t1 * r12.x + t2 * r23.x + t3 * r34.x);
-        const double f1y = g1 * (t1 * r12.y + t2 * r23.y + t3 * r34.y);
-        const double f1z = g1 * (t1 * r12.z + t2 * r23.z + t3 * r34.z);
-        const double f4x = g4 * (t4 * r12.x + t5 * r23.x + t6 * r34.x);
-        const double f4y = g4 * (t4 * r12.y + t5 * r23.y + t6 * r34.y);
-        const double f4z = g4 * (t4 * r12.z + t5 * r23.z + t6 * r34.z);
-        const double u = c12 / c22, v = c23 / c22;
-        add_force(a.facc, a.status, d.x, f1x, f1y, f1z);
-        add_force(a.facc, a.status, d.y, -(1.0 + u) * f1x + v * f4x, -(1.0 + u) * f1y + v * f4y,
-                  -(1.0 + u) * f1z + v * f4z);
-        add_force(a.facc, a.status, d.z, u * f1x - (1.0 + v) * f4x, u * f1y - (1.0 + v) * f4y,
-                  u * f1z - (1.0 + v) * f4z);
-        add_force(a.facc, a.status, d.w, f4x, f4y, f4z);
+        // Blondel-Karplus: F = x1 - x2, G = x2 - x3, H = x4 - x3
+        const F3 F = rvec(a.pos, d.x, d.y, L, h);
+        const F3 G = rvec(a.pos, d.y, d.z, L, h);
+        const F3 Hm = rvec(a.pos, d.z, d.w, L, h);  // x3 - x4 = -H
+        const F3 H{-Hm.x, -Hm.y, -Hm.z};
+        const F3 A = crossf(F, G), B = crossf(H, G);
+        const float A2 = dotf(A, A), B2 = dotf(B, B);
+        const float Gn = __fsqrt_rn(dotf(G, G));
+        if (!(A2 > 0.0f) || !(B2 > 0.0f) || !(Gn > 0.0f)) return;  // collinear triple
+        const float cphi = dotf(A, B);
+        const float sphi = __fdiv_rn(dotf(crossf(B, A), G), Gn);
+        if (sphi == 0.0f) return;  // exactly planar: |cos phi| = 1 in the reference
+        const float phi_u = atan2f(fabsf(sphi), cphi);
+        const float4 p = a.dih_par[ty];
+        // -dU/dphi (signed phi)
+        const float g = p.x * p.y * sinf(fmaf(p.x, phi_u, -p.z)) * (sphi > 0.0f ? 1.0f : -1.0f);
+        const float FG = dotf(F, G), HG = dotf(H, G);
+        const float ga = __fdiv_rn(g * Gn, A2);   // force on x1 = -g Gn / A2 A ...
+        const float gb = __fdiv_rn(g * Gn, B2);
+        const float fa = __fdiv_rn(g * FG, A2 * Gn);
+        const float fb = __fdiv_rn(g * HG, B2 * Gn);
+        const F3 f1 = scalef(-ga, A);
+        const F3 f4 = scalef(gb, B);
+        const F3 f2{fmaf(ga + fa, A.x, -fb * B.x), fmaf(ga + fa, A.y, -fb * B.y), fmaf(ga + fa, A.z, -fb * B.z)};
+        const F3 f3{fmaf(fb - gb, B.x, -fa * A.x), fmaf(fb - gb, B.y, -fa * A.y), fmaf(fb - gb, B.z, -fa * A.z)};
+        add(d.x, f1);
+        add(d.y, f2);
+        add(d.z, f3);
+        add(d.w, f4);
     }
+}
+
+__global__ void bonded_kernel(BondedArgs a) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    bonded_term(a, idx, FixAdd{a.facc, a.status});
 }
 
 constexpr int kUsThreads = 256;
 
-__global__ void __launch_bounds__(kUsThreads) umbrella_kernel(UmbrellaArgs a) {
-    __shared__ double s_red[6][kUsThreads];
-    __shared__ double s_f[4];
-    const int w = a.us_windows[blockIdx.x];
+// Centre of mass of both restraint groups of window w in FP64, reduced by one
+// block in a fixed order (us_force_cuda.cu:14-48, whose __syncthreads only
+// orders a single block); writes the COMs and the CV of the window and returns
+// (in `sf`, on every thread) the minimum-image COM axis r and (|r| - x0)/|r|.
+__device__ void umbrella_com_block(const UmbrellaArgs &a, int w, double *s_red /* [6][kUsThreads] */,
+                                   double *sf /* [4], shared */) {
     const WinDev W = a.win[w];
     double c[6] = {0, 0, 0, 0, 0, 0};
-    for (int b = threadIdx.x; b < W.n_bias; b += kUsThreads) {
+    for (int b = threadIdx.x; b < W.n_bias; b += blockDim.x) {
         const int2 e = a.bias[W.bias_off + b];
         const float4 x = a.pos[e.x];
         const double m = a.mfrac[W.bias_off + b];
@@ -237,47 +266,72 @@ __global__ void __launch_bounds__(kUsThreads) umbrella_kernel(UmbrellaArgs a) {
         c[o + 1] += m * x.y;
         c[o + 2] += m * x.z;
     }
-    for (int k = 0; k < 6; ++k) s_red[k][threadIdx.x] = c[k];
+    for (int k = 0; k < 6; ++k) s_red[k * kUsThreads + threadIdx.x] = c[k];
+    for (int t = threadIdx.x + blockDim.x; t < kUsThreads; t += blockDim.x)
+        for (int k = 0; k < 6; ++k) s_red[k * kUsThreads + t] = 0.0;
     __syncthreads();
     for (int stride = kUsThreads / 2; stride > 0; stride >>= 1) {
-        if (threadIdx.x < stride)
-            for (int k = 0; k < 6; ++k) s_red[k][threadIdx.x] += s_red[k][threadIdx.x + stride];
+        for (int t = threadIdx.x; t < stride; t += blockDim.x)
+            for (int k = 0; k < 6; ++k) s_red[k * kUsThreads + t] += s_red[k * kUsThreads + t + stride];
         __syncthreads();
     }
     if (threadIdx.x == 0) {
         const double L = W.box, hh = 0.5 * W.box;
         double r[3];
         for (int k = 0; k < 3; ++k) {
-            double v = s_red[k][0] - s_red[3 + k][0];
+            double v = s_red[k * kUsThreads] - s_red[(3 + k) * kUsThreads];
             if (v > hh) v -= L;
             else if (v < -hh) v += L;
             r[k] = v;
         }
         const double d = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
-        for (int k = 0; k < 6; ++k) a.com[6 * (long long)w + k] = s_red[k][0];
+        for (int k = 0; k < 6; ++k) a.com[6 * (long long)w + k] = s_red[k * kUsThreads];
         a.cv[w] = d;
-        s_f[0] = r[0];
-        s_f[1] = r[1];
-        s_f[2] = r[2];
-        s_f[3] = (d - (double)W.us_x0) / d;
+        sf[0] = r[0];
+        sf[1] = r[1];
+        sf[2] = r[2];
+        sf[3] = (d - (double)W.us_x0) / d;
     }
     __syncthreads();
+}
+
+// Restraint force on bias entry b of window w: -+k (d - x0)/d m_i/M_g r
+// (us_class.cpp:153-154 sign per group), in the accumulator's fixed point.
+__device__ __forceinline__ void umbrella_entry_fix(const UmbrellaArgs &a, const WinDev &W, int b, const double *sf,
+                                                   long long out[3]) {
+    const int2 e = a.bias[W.bias_off + b];
+    const double ku = e.y == 0 ? -(double)W.us_k : (double)W.us_k;
+    const double pf = ku * sf[3] * (double)a.mfrac[W.bias_off + b];
+    const double f[3] = {pf * sf[0], pf * sf[1], pf * sf[2]};
+    const double m = fmax(fabs(f[0]), fmax(fabs(f[1]), fabs(f[2])));
+    if (!(m <= (double)kFixLimit)) atomicOr(a.status, (m != m || isinf(m)) ? kStatusNonFinite : kStatusOverflow);
+    for (int k = 0; k < 3; ++k) out[k] = __double2ll_rn(f[k] * 4294967296.0);
+}
+
+__global__ void __launch_bounds__(kUsThreads) umbrella_kernel(UmbrellaArgs a) {
+    __shared__ double s_red[6 * kUsThreads];
+    __shared__ double s_f[4];
+    const int w = a.us_windows[blockIdx.x];
+    umbrella_com_block(a, w, s_red, s_f);
+    const WinDev W = a.win[w];
     for (int b = threadIdx.x; b < W.n_bias; b += kUsThreads) {
-        const int2 e = a.bias[W.bias_off + b];
-        const double ku = e.y == 0 ? -(double)W.us_k : (double)W.us_k;  // us_class.cpp:153-154
-        const double pf = ku * s_f[3] * (double)a.mfrac[W.bias_off + b];
-        add_force(a.facc, a.status, e.x, pf * s_f[0], pf * s_f[1], pf * s_f[2]);
+        long long f[3];
+        umbrella_entry_fix(a, W, b, s_f, f);
+        unsigned long long *acc = a.facc + 3 * (long long)a.bias[W.bias_off + b].x;
+        for (int k = 0; k < 3; ++k) atomicAdd(acc + k, (unsigned long long)f[k]);
     }
 }
 
-__device__ __forceinline__ void leapfrog_atom(const LeapfrogArgs &a, int i, uint32_t step);
+// Leapfrog of atom i (leapfrog_cuda.cu:33-68) from the accumulated force
+// plus `extra` (fixed point), which it reads through L2 and clears.
+__device__ __forceinline__ void leapfrog_atom(const LeapfrogArgs &a, int i, uint32_t step, const long long *extra);
 
 // Every block reads the step counter first; the last block to finish
 // advances it (no block waits on another).
 __global__ void leapfrog_kernel(LeapfrogArgs a) {
     const uint32_t step = *a.step_ptr;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < a.n_atoms) leapfrog_atom(a, i, step);
+    if (i < a.n_atoms) leapfrog_atom(a, i, step, nullptr);
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
@@ -290,13 +344,16 @@ __global__ void leapfrog_kernel(LeapfrogArgs a) {
     }
 }
 
-__device__ __forceinline__ void leapfrog_atom(const LeapfrogArgs &a, int i, uint32_t step) {
+__device__ __forceinline__ void leapfrog_atom(const LeapfrogArgs &a, int i, uint32_t step, const long long *extra) {
     const int w = a.atom_win[i];
     const WinDev W = a.win[w];
     unsigned long long *acc = a.facc + 3 * (long long)i;
-    const float fx = (float)((double)(long long)acc[0] * kFixInv);
-    const float fy = (float)((double)(long long)acc[1] * kFixInv);
-    const float fz = (float)((double)(long long)acc[2] * kFixInv);
+    long long s[3] = {(long long)__ldcg(acc + 0), (long long)__ldcg(acc + 1), (long long)__ldcg(acc + 2)};
+    if (extra)
+        for (int k = 0; k < 3; ++k) s[k] += extra[k];
+    const float fx = (float)((double)s[0] * kFixInv);
+    const float fy = (float)((double)s[1] * kFixInv);
+    const float fz = (float)((double)s[2] * kFixInv);
     acc[0] = 0ull;
     acc[1] = 0ull;
     acc[2] = 0ull;
@@ -337,6 +394,88 @@ __device__ __forceinline__ void leapfrog_atom(const LeapfrogArgs &a, int i, uint
         atomicOr(a.status, kStatusNonFinite);
     a.vel[i] = v;
     a.pos[i] = x;
+}
+
+// Grid-wide barrier of a cooperative launch (every block resident): arrival
+// count and generation word, both zero at rest.  The wait is bounded: after
+// kBarrierSpins polls the block gives up, flags kStatusTimeout and returns
+// false, and the caller skips the work that needed the barrier.
+constexpr long long kBarrierSpins = 1LL << 22;
+__device__ bool grid_barrier(unsigned int *bar, int *status) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned int *gen = bar + 1;
+        const unsigned int g = *gen;
+        __threadfence();
+        int ok = 1;
+        if (atomicAdd(bar, 1u) == gridDim.x - 1) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            long long spins = 0;
+            while (*gen == g) {
+                if (++spins > kBarrierSpins) {
+                    atomicOr(status, kStatusTimeout);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// The fused integrator: bonded terms, the umbrella restraint and leapfrog in
+// one cooperative launch.  Phase 1: blocks take the restrained windows' FP64
+// COMs (one block per window, fixed order) and every thread a share of the
+// bonded terms (fixed-point atomics, the bonded kernel's term code).  Grid
+// barrier.  Phase 2: every atom adds its restraint force from its window's
+// COM axis (the umbrella kernel's fixed-point values, no atomics) and is
+// integrated; block 0 advances the step counter.  The integer sums are those
+// of the separate bonded, umbrella and leapfrog kernels, so the trajectory is
+// bit-identical to theirs.
+__global__ void __launch_bounds__(kUsThreads) integrator_kernel(IntegratorArgs a) {
+    __shared__ double s_red[6 * kUsThreads];
+    __shared__ double s_f[4];
+    const uint32_t step = *a.lf.step_ptr;
+    for (int u = blockIdx.x; u < a.us.n_us_windows; u += gridDim.x) {
+        const int w = a.us.us_windows[u];
+        umbrella_com_block(a.us, w, s_red, s_f);
+        if (threadIdx.x == 0) {
+            a.usf[2 * w] = make_double2(s_f[0], s_f[1]);
+            a.usf[2 * w + 1] = make_double2(s_f[2], s_f[3]);
+        }
+        __syncthreads();
+    }
+    const long long n_terms = (a.bonded.do_bonds ? a.bonded.n_bonds : 0) +
+                              (a.bonded.do_angles ? a.bonded.n_angles : 0) +
+                              (a.bonded.do_dihs ? a.bonded.n_dihs : 0);
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const FixAdd add{a.bonded.facc, a.bonded.status};
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n_terms; t += stride)
+        bonded_term(a.bonded, t, add);
+    if (!grid_barrier(a.bar, a.lf.status)) return;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < a.lf.n_atoms; i += stride) {
+        long long extra[3] = {0, 0, 0};
+        for (int k = a.bias_start[i]; k < a.bias_start[i + 1]; ++k) {
+            const int b = a.bias_by_atom[k];  // global bias entry
+            const int w = a.lf.atom_win[i];
+            const WinDev W = a.us.win[w];
+            const double2 q0 = __ldcg(a.usf + 2 * w), q1 = __ldcg(a.usf + 2 * w + 1);
+            const double sf[4] = {q0.x, q0.y, q1.x, q1.y};
+            long long f[3];
+            umbrella_entry_fix(a.us, W, b - W.bias_off, sf, f);
+            for (int c = 0; c < 3; ++c) extra[c] += f[c];
+        }
+        leapfrog_atom(a.lf, (int)i, step, extra);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *a.lf.step_ptr = step + 1u;
 }
 
 // Neighbour list of one window: one warp per atom, partners scanned in
@@ -418,6 +557,32 @@ void launch_bonded(const BondedArgs &a, cudaStream_t s) {
 
 void launch_umbrella(const UmbrellaArgs &a, cudaStream_t s) {
     if (a.n_us_windows > 0) umbrella_kernel<<<a.n_us_windows, kUsThreads, 0, s>>>(a);
+}
+
+int integrator_block_threads() { return kUsThreads; }
+
+int integrator_max_blocks() {
+    int dev = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, integrator_kernel, kUsThreads, 0) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return sms * per_sm;
+}
+
+cudaError_t launch_integrator(const IntegratorArgs &a, int grid, cudaStream_t s) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(kUsThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, integrator_kernel, a);
 }
 
 void launch_leapfrog(const LeapfrogArgs &a, cudaStream_t s) {

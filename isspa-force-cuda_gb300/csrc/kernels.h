@@ -122,6 +122,19 @@ struct LeapfrogArgs {
     int *status;
 };
 
+// Fused integrator: the bonded terms, the umbrella restraint and leapfrog of a
+// step in one cooperative launch (a grid barrier between the force terms and
+// the update).
+struct IntegratorArgs {
+    BondedArgs bonded;
+    UmbrellaArgs us;
+    LeapfrogArgs lf;
+    const int *bias_start;     // [Ntot+1]: atom i's bias entries are bias_by_atom[bias_start[i]..bias_start[i+1])
+    const int *bias_by_atom;   // global bias entry indices, grouped by atom
+    double2 *usf;              // [n_windows][2]: COM axis r and (|r| - x0)/|r| of the step
+    unsigned int *bar;         // grid barrier: arrival count, generation (zero at rest)
+};
+
 struct ListArgs {
     const float4 *pos;
     const int *excl_start;
@@ -199,6 +212,11 @@ void launch_nonbond(const NonbondArgs &a, cudaStream_t s);
 void launch_bonded(const BondedArgs &a, cudaStream_t s);
 void launch_umbrella(const UmbrellaArgs &a, cudaStream_t s);
 void launch_leapfrog(const LeapfrogArgs &a, cudaStream_t s);
+// Cooperative launch of the fused integrator on `grid` blocks (at most
+// integrator_max_blocks()); returns the launch's error code.
+cudaError_t launch_integrator(const IntegratorArgs &a, int grid, cudaStream_t s);
+int integrator_max_blocks();
+int integrator_block_threads();
 void launch_neighbor_list(const ListArgs &a, cudaStream_t s);
 // Up to three float4 arrays of n elements copied element-wise (a null source
 // skips its pair): state moved between the engine's device arrays and

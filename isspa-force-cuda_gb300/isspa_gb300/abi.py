@@ -51,7 +51,7 @@ class EngineOptions(C.Structure):
     _fields_ = [("isspa_terms", C.c_int), ("nonbond_terms", C.c_int), ("use_graph", C.c_int),
                 ("field_split", C.c_int), ("force_chunk", C.c_int), ("mem_cap", C.c_size_t),
                 ("force_atoms_per_thread", C.c_int), ("force_tail_chunk", C.c_int),
-                ("field_vote", C.c_int), ("force_vote", C.c_int)]
+                ("field_vote", C.c_int), ("force_vote", C.c_int), ("integrator", C.c_int)]
 
 
 class RunConfig(C.Structure):
@@ -72,11 +72,13 @@ class NoallocInputs(C.Structure):
                 ("g_table", C.c_void_p), ("e_table", C.c_void_p), ("f_table", C.c_void_p),
                 ("g_r0", C.c_float), ("g_dr", C.c_float), ("e_r0", C.c_float), ("e_dr", C.c_float),
                 ("f_r0", C.c_float), ("f_dr", C.c_float), ("box", C.c_float),
-                ("seed", C.c_uint64), ("step", C.c_uint32), ("terms", C.c_int)]
+                ("seed", C.c_uint64), ("step", C.c_uint32), ("terms", C.c_int), ("status_out", C.c_void_p)]
 
 
 NOALLOC_SCRATCH_BYTES = 16 << 20
-SHAPE_COUNT = 11  # ISSPA_SHAPE_COUNT
+# ISSPA_NOALLOC_STATUS_* bits written to isspa_noalloc_inputs.status_out
+NOALLOC_STATUS_OVERFLOW, NOALLOC_STATUS_NONFINITE, NOALLOC_STATUS_BOUNDS = 1, 2, 4
+SHAPE_COUNT = 12  # ISSPA_SHAPE_COUNT
 TERMS_NONE = -1  # ISSPA_TERMS_NONE: switches the IS-SPA or nonbond pass off
 
 # isspa_energies components (the ISSPA_E_* enum), kcal/mol
@@ -121,6 +123,7 @@ SIGNATURES = [
     ("isspa_host_free", None, [_P]),
     ("isspa_synchronize", C.c_int, [_P]),
     ("isspa_device_status", C.c_int, [_P, C.c_int]),
+    ("isspa_debug_stall_barrier", C.c_int, [_P]),
     ("isspa_set_positions", C.c_int, [_P, _P, C.c_int]),
     ("isspa_get_positions", C.c_int, [_P, _P, C.c_int]),
     ("isspa_set_velocities", C.c_int, [_P, _P, C.c_int]),

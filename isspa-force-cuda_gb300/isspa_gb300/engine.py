@@ -24,7 +24,7 @@ class Engine:
     def __init__(self, windows: "System | Sequence[System]", isspa_terms: int = 7,
                  nonbond_terms: int = 7, use_graph: bool = True, field_split: int = 0,
                  force_chunk: int = 0, mem_cap: int = 0, force_atoms_per_thread: int = 0,
-                 force_tail_chunk: int = 0, field_vote: int = 0, force_vote: int = 0):
+                 force_tail_chunk: int = 0, field_vote: int = 0, force_vote: int = 0, integrator: int = 0):
         if isinstance(windows, System):
             windows = [windows]
         self.windows = list(windows)
@@ -44,6 +44,7 @@ class Engine:
         opt.force_tail_chunk = int(force_tail_chunk)
         opt.field_vote = int(field_vote)
         opt.force_vote = int(force_vote)
+        opt.integrator = int(integrator)
         h = C.c_void_p()
         abi.check(L.isspa_engine_create(descs, len(self.windows), C.byref(opt), C.byref(h)), "engine create")
         self._h = h
@@ -57,7 +58,7 @@ class Engine:
         abi.check(abi.lib().isspa_engine_shapes(self._h, v), "shapes")
         keys = ("field_split", "field_tiles", "force_chunk", "force_items", "nonbond_items",
                 "nonbond_partners_per_item", "sms", "force_atoms_per_thread", "force_tail_chunk",
-                "field_vote", "force_vote")
+                "field_vote", "force_vote", "integrator")
         return dict(zip(keys, list(v)))
 
     def autotune(self, reps: int = 3) -> dict:
@@ -134,7 +135,7 @@ class Engine:
         abi.check(abi.lib().isspa_time_steps(self._h, int(nsteps), int(flush_bytes), C.byref(ms)), "time")
         return ms.value
 
-    KERNELS = ("field", "force", "nonbond", "bonded", "umbrella", "leapfrog")
+    KERNELS = ("field", "force", "nonbond", "bonded", "umbrella", "leapfrog", "integrator")
 
     def time_steps_detailed(self, nsteps: int, flush_bytes: int = 0):
         """Device time of `nsteps` graph-replayed steps and of every kernel in them."""

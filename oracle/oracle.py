@@ -176,7 +176,8 @@ class Oracle:
         lib().orc_nonbond(C.byref(self.nsys), int(terms), _p(f))
         return f
 
-    def bonded(self, with_14: bool = True) -> np.ndarray:
+    def bonded(self, with_14: bool = True, bonds: bool = True, angles: bool = True,
+               dihedrals: bool = True) -> np.ndarray:
         s = self.s
         f = np.zeros((self.n, 3))
         L = lib()
@@ -185,11 +186,11 @@ class Oracle:
         da = _i32(s.dih_atoms); dt = _i32(s.dih_types); dp = _f32(s.dih_params)
         sc = _f32(s.scaled14)
         ljt = _i32(s.lj_type); nbp = _i32(s.nb_parm_index); lj = self.lj
-        if len(ba):
+        if bonds and len(ba):
             L.orc_bonds(len(ba), _p(ba), _p(bp), _p(self.pos), C.c_float(s.box), _p(f))
-        if len(aa):
+        if angles and len(aa):
             L.orc_angles(len(aa), _p(aa), _p(ap), _p(self.pos), C.c_float(s.box), _p(f))
-        if len(da):
+        if dihedrals and len(da):
             L.orc_dihedrals(len(da), _p(da), _p(dt), _p(dp), _p(sc), _p(ljt), _p(nbp),
                             int(s.n_lj_types), _p(lj), _p(self.pos), C.c_float(s.box),
                             int(with_14), _p(f))

@@ -1,0 +1,158 @@
+"""Bonded terms (FP32) and the fused integrator, through the C ABI.
+
+* Near-planar torsions: chains laid out as planar zig-zags (bonds 1.5 A,
+  angles 110 deg, trans with some cis torsions) lifted out of the plane by
+  noise of 1e-2 to 1e-4 A, so every torsion angle lies within ~1e-2 to 1e-4
+  rad of 0 or pi, where the reference's acos / (1/sin phi) form loses its
+  precision in FP32.  Each bonded term is compared per atom with the FP64
+  oracle (tests/parity.py measures, 1e-5).
+* The fused integrator (bonded, umbrella and leapfrog in one cooperative
+  kernel) gives the separate kernels' trajectory bit for bit: a plain
+  system, a restrained batch of windows, and the reference's ADI2 inputs
+  with its umbrella restraint.
+* The autotuner's integrator choice leaves the state where it was.
+* The grid barrier's bounded wait: a barrier left mid-count runs out,
+  the step reports ISSPA_ERR_TIMEOUT without a fault, and the same engine
+  steps on cleanly after the status is reset.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import isspa_gb300 as ig
+import oracle as O
+from isspa_gb300 import abi
+from parity import check_force
+
+pytestmark = pytest.mark.gpu
+
+
+def planar_chain(n, rng, origin):
+    """A zig-zag of n atoms in the plane z = origin[2]: bond 1.5 A, angle 110
+    deg; mostly alternating turns (trans), a same-direction turn (cis) now and
+    then but never twice in a row."""
+    bond, theta = 1.5, math.radians(110.0)
+    x = np.zeros((n, 3))
+    x[0] = origin
+    ang = rng.uniform(0, 2 * math.pi)
+    x[1] = x[0] + bond * np.array([math.cos(ang), math.sin(ang), 0.0])
+    turn, last_cis = 1.0, True
+    for i in range(2, n):
+        cis = (not last_cis) and rng.random() < 0.2
+        if not cis:
+            turn = -turn
+        last_cis = cis
+        ang += turn * (math.pi - theta)
+        x[i] = x[i - 1] + bond * np.array([math.cos(ang), math.sin(ang), 0.0])
+    return x
+
+
+@pytest.fixture(scope="module")
+def flat_systems():
+    out = {}
+    base = ig.synth.make_system(2, 22, 60.0, 20, seed=12, ff=ig.synth.forcefield(n_mc=20))
+    for noise in (1e-2, 1e-3, 1e-4):
+        rng = np.random.default_rng(7)
+        s = base.copy()
+        pos = s.pos.copy()
+        pos[:22, :3] = planar_chain(22, rng, np.array([20.0, 20.0, 15.0]))
+        pos[22:, :3] = planar_chain(22, rng, np.array([20.0, 20.0, 40.0]))
+        pos[:, 2] += rng.uniform(-noise, noise, len(pos))
+        s.pos = pos.astype(np.float32)
+        out[noise] = s
+    return out
+
+
+@pytest.mark.parametrize("noise", [1e-2, 1e-3, 1e-4])
+def test_near_planar_torsions_match_fp64_oracle(flat_systems, noise):
+    s = flat_systems[noise]
+    o = O.Oracle(s)
+    eng = ig.Engine(s)
+    for name, call, ref in [("dihedrals + 1-4", eng.dih_force, o.bonded(bonds=False, angles=False)),
+                            ("angles", eng.angle_force, o.bonded(bonds=False, dihedrals=False)),
+                            ("bonds", eng.bond_force, o.bonded(angles=False, dihedrals=False))]:
+        eng.zero_forces()
+        call()
+        check_force(eng.forces(), ref, f"near-planar chains (z noise {noise:g} A), {name}")
+    eng.zero_forces()
+    eng.bond_force()
+    eng.angle_force()
+    eng.dih_force()
+    check_force(eng.forces(), o.bonded(), f"near-planar chains (z noise {noise:g} A), all bonded")
+    assert eng.device_status() == 0
+
+
+def _trajectories(windows, steps, **opts):
+    out = []
+    for integ in (1, 2):
+        eng = ig.Engine(windows, integrator=integ, **opts)
+        assert eng.shapes()["integrator"] == integ
+        eng.step(steps)
+        out.append((eng.positions(), eng.velocities(), eng.forces_out() if hasattr(eng, "forces_out") else None,
+                    eng.us_com(), eng.get_step(), eng.device_status()))
+        eng.close()
+    return out
+
+
+@pytest.mark.parametrize("which", ["medium", "batched-umbrella", "adi2-umbrella"])
+def test_fused_integrator_bit_identical(which, adi2):
+    if which == "medium":
+        wins = ig.synth.make_system(12, 22, 34.0, 20, seed=21, ff=ig.synth.forcefield(n_mc=20))
+        wins.pnu = 0.2
+    elif which == "batched-umbrella":
+        wins = ig.synth.config_batched(n_windows=3, seed=9)
+    else:
+        s = adi2.copy()
+        s.n_mc = 20
+        s.us_on = 1
+        s.bias_list = np.array([(i, 0) for i in range(22)] + [(22 + i, 1) for i in range(22)], np.int32)
+        s.us_k, s.us_x0 = 20.0, 10.0
+        s.pnu = 0.05
+        wins = s
+    (p1, v1, _, c1, st1, ds1), (p2, v2, _, c2, st2, ds2) = _trajectories(wins, 12)
+    assert ds1 == 0 and ds2 == 0
+    assert st1 == st2 == 12
+    assert np.array_equal(p1, p2)
+    assert np.array_equal(v1, v2)
+    assert np.array_equal(c1[0], c2[0]) and np.array_equal(c1[1], c2[1])
+
+
+def test_autotune_restores_state():
+    s = ig.synth.config_small(seed=1)
+    a = ig.Engine(s)
+    b = ig.Engine(s)
+    a.step(3)
+    b.step(3)
+    sh = a.autotune()
+    assert sh["integrator"] in (1, 2)
+    assert a.get_step() == 3
+    assert np.array_equal(a.positions(), b.positions())
+    assert np.array_equal(a.velocities(), b.velocities())
+    a.step(5)
+    b.step(5)
+    assert np.array_equal(a.positions(), b.positions())  # shapes move no result of a step here
+
+
+def test_fused_integrator_barrier_timeout_is_reported():
+    """A grid barrier left mid-count (as after a lost block) never completes:
+    every block's bounded wait runs out, the step reports ISSPA_ERR_TIMEOUT,
+    nothing faults, and after the status reset the engine steps on cleanly
+    from a valid state."""
+    s = ig.synth.config_small(seed=1)
+    eng = ig.Engine(s, integrator=2)
+    ref = ig.Engine(s, integrator=2)
+    L = abi.lib()
+    abi.check(L.isspa_debug_stall_barrier(eng._h), "stall barrier")
+    eng.step(1)
+    assert eng.device_status() == abi.ERR_TIMEOUT
+    assert eng.device_status(reset=True) == abi.ERR_TIMEOUT
+    assert eng.device_status() == 0
+    eng.set_positions(s.pos)
+    eng.set_velocities(s.vel)
+    eng.set_step(0)
+    eng.zero_forces()
+    eng.step(10)
+    ref.step(10)
+    assert eng.device_status() == 0
+    assert np.array_equal(eng.positions(), ref.positions())

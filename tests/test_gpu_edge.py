@@ -12,17 +12,13 @@ import pytest
 
 import isspa_gb300 as ig
 import oracle as O
+from parity import check_force
 
 pytestmark = pytest.mark.gpu
-TOL = 2e-5
 
 
 def _sys(n_chains, length, n_mc, box=30.0, seed=3):
     return ig.synth.make_system(n_chains, length, box, n_mc, seed=seed, ff=ig.synth.forcefield(n_mc=n_mc))
-
-
-def _nrel(a, b):
-    return float(np.abs(np.asarray(a, np.float64) - b).max() / max(np.abs(b).max(), 1e-300))
 
 
 @pytest.mark.parametrize("shape", [(1, 1, 20), (2, 1, 20), (1, 22, 1), (2, 22, 1)],
@@ -32,8 +28,7 @@ def test_small_systems_match_oracle(shape):
     eng = ig.Engine(s)
     f = eng.compute_forces()
     ref, _, _ = O.Oracle(s).total_force(seed=s.seed, step=0)
-    print(shape, "normwise", _nrel(f, ref))
-    assert _nrel(f, ref) < TOL
+    check_force(f, ref, f"{shape}")
     eng.zero_forces()
     eng.step(100)
     assert eng.device_status() == 0
@@ -47,7 +42,7 @@ def test_ragged_batch_matches_oracle():
     off = 0
     for w, s in enumerate(wins):
         ref, _, _ = O.Oracle(s).total_force(seed=s.seed, step=0, window=w)
-        assert _nrel(f[off:off + s.n_atoms], ref) < TOL, w
+        check_force(f[off:off + s.n_atoms], ref, f"ragged batch window {w}")
         off += s.n_atoms
     eng.zero_forces()
     eng.step(100)
