@@ -124,6 +124,8 @@ typedef struct isspa_engine_options {
                             2 = one fused cooperative kernel for bonded, umbrella and
                             leapfrog after the force passes (same results bit for bit);
                             0 => 1 until isspa_autotune times both and keeps the faster */
+    int nonbond_chunk;   /* partners per nonbond work item (rounded up to a multiple of 128;
+                            the results do not depend on it); 0 => auto */
 } isspa_engine_options;
 
 #define ISSPA_TERMS_NONE (-1)
@@ -199,7 +201,8 @@ int isspa_engine_shapes(const isspa_engine *e, int shape[ISSPA_SHAPE_COUNT]);
  * workload with CUDA events (reps launches each), keeps the fastest of each
  * and reports the result as isspa_engine_shapes does.  When the options leave
  * the integrator open (0), it then times single-step graph replays with the
- * separate and the fused integrator and keeps the faster; positions,
+ * separate and the fused integrator and keeps the faster (the nonbond
+ * partners per item are timed too); positions,
  * velocities and the step counter are restored.  Clears the force
  * accumulator; invalidates captured graphs. */
 int isspa_autotune(isspa_engine *e, int reps, int shape[ISSPA_SHAPE_COUNT]);

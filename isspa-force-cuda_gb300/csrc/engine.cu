@@ -104,6 +104,7 @@ struct isspa_engine {
     int n_nb_items = 0, nb_chunk = 0, n_sms = 0;
     int4 *bonds = nullptr, *angles = nullptr, *dihs = nullptr;
     float2 *bond_par = nullptr, *angle_par = nullptr, *sc14 = nullptr;
+    float4 *angle_cs = nullptr;
     float4 *dih_par = nullptr;
     int *dih_type = nullptr;
     int n_bonds = 0, n_angles = 0, n_dihs = 0;
@@ -279,6 +280,42 @@ struct isspa_engine {
         force_tail = Ct;
     }
 
+    long long nonbond_items_for(long long J) const {
+        long long n = 0;
+        for (const WinDev &d : win_h) n += ((d.n_atoms + 127) / 128) * ((d.n_atoms + J - 1) / J);
+        return n;
+    }
+    // The longest partner stretch (fewest stage set-ups and atomics) whose
+    // items still fill two waves of resident blocks; 128 when none does.
+    int default_nonbond_chunk() const {
+        const long long slots = (long long)n_sms * std::max(1, nonbond_blocks_per_sm(n_lj_types));
+        for (int J : {4096, 2048, 1024, 768, 512, 384, 256})
+            if (nonbond_items_for(J) >= 2 * slots) return J;
+        return 128;
+    }
+    // Nonbond work items, partner-chunk-major: blocks that run together add
+    // into different receiving tiles.  Per-stage sums start at multiples of
+    // 128 partners from the window's first atom, so J moves no result.
+    void set_nonbond_chunk(int J) {
+        J = std::max(128, ((J + 127) / 128) * 128);
+        std::vector<int4> items;
+        std::vector<int> nj;
+        for (int w : order) {
+            const WinDev &d = win_h[w];
+            for (int j = 0; j < d.n_atoms; j += J)
+                for (int a = 0; a < d.n_atoms; a += 128) {
+                    items.push_back(make_int4(w, d.atom_off + a, std::min(128, d.n_atoms - a), d.atom_off + j));
+                    nj.push_back(std::min(J, d.n_atoms - j));
+                }
+        }
+        release(nb_items);
+        release(nb_nj);
+        nb_items = upload(items);
+        nb_nj = upload(nj);
+        n_nb_items = (int)items.size();
+        nb_chunk = J;
+    }
+
     ~isspa_engine() {
         if (stream) cudaStreamSynchronize(stream);
         if (graph1) cudaGraphExecDestroy(graph1);
@@ -379,6 +416,7 @@ struct isspa_engine {
         a.angles = angles;
         a.n_angles = n_angles;
         a.angle_par = angle_par;
+        a.angle_cs = angle_cs;
         a.dihs = dihs;
         a.dih_type = dih_type;
         a.n_dihs = n_dihs;
@@ -819,22 +857,9 @@ void build(isspa_engine &E, const std::vector<isspa_host_system> &ws) {
     E.force_apt = E.opt.force_atoms_per_thread == 2 ? 2 : 1;
     E.set_force_chunk(E.opt.force_chunk > 0 ? E.opt.force_chunk : E.default_force_chunk(),
                       std::max(0, E.opt.force_tail_chunk));
-    // nonbond items: 128 i-atoms x J partners
-    std::vector<int4> nitems;
-    std::vector<int> nnj;
-    long long npairs = 0;
-    for (int w = 0; w < W; ++w) npairs += (long long)ws[w].n_atoms * ws[w].n_atoms;
-    int J = (int)std::max<long long>(128, std::min<long long>(4096, ((npairs / (128LL * 608) + 127) / 128) * 128));
-    for (int w : E.order) {
-        const WinDev &d = E.win_h[w];
-        for (int a = 0; a < d.n_atoms; a += 128)
-            for (int j = 0; j < d.n_atoms; j += J) {
-                nitems.push_back(make_int4(w, d.atom_off + a, std::min(128, d.n_atoms - a), d.atom_off + j));
-                nnj.push_back(std::min(J, d.n_atoms - j));
-            }
-    }
-    E.n_nb_items = (int)nitems.size();
-    E.nb_chunk = J;
+    // nonbond items: 128 i-atoms x J partners (J a multiple of 128)
+    E.set_nonbond_chunk(E.opt.nonbond_chunk > 0 ? ((E.opt.nonbond_chunk + 127) / 128) * 128
+                                                : E.default_nonbond_chunk());
 
     // ---- upload ----
     E.pos = E.upload(pos);
@@ -853,14 +878,23 @@ void build(isspa_engine &E, const std::vector<isspa_host_system> &ws) {
     E.ljab = E.upload(ljab);
     E.excl_start = E.upload(ex_start);
     E.excl = E.upload(ex_flat);
-    E.nb_items = E.upload(nitems);
-    E.nb_nj = E.upload(nnj);
     E.bonds = E.upload(bonds);
     E.angles = E.upload(angles);
     E.dihs = E.upload(dihs);
     E.dih_type = E.upload(dih_type);
     E.bond_par = E.upload(bond_par);
     E.angle_par = E.upload(angle_par);
+    {
+        // cos / sin of each equilibrium angle (the float parameter, exactly)
+        // as double-float pairs for the bend theta - theta0
+        std::vector<float4> cs(angle_par.size());
+        for (size_t t = 0; t < angle_par.size(); ++t) {
+            const double th = (double)angle_par[t].y, c = std::cos(th), sn = std::sin(th);
+            const float ch = (float)c, sh = (float)sn;
+            cs[t] = make_float4(ch, (float)(c - (double)ch), sh, (float)(sn - (double)sh));
+        }
+        E.angle_cs = E.upload(cs);
+    }
     E.dih_par = E.upload(dih_par);
     E.sc14 = E.upload(sc14);
     E.us_windows = E.upload(us_windows);
@@ -1373,6 +1407,23 @@ int isspa_autotune(isspa_engine *e, int reps, int shape[ISSPA_SHAPE_COUNT]) {
             e->force_vote = 1;
             const float voted = time_it([&] { launch_force(e->force_args(), e->stream); });
             e->force_vote = voted < plain ? 1 : 0;
+        }
+        // nonbond pass: partner stretches per item (results do not move)
+        if (e->opt.nonbond_terms && e->n_nb_items > 0) {
+            int maxN = 0;
+            for (const WinDev &d : e->win_h) maxN = std::max(maxN, d.n_atoms);
+            float bestn = 1e30f;
+            int bestJ = e->nb_chunk;
+            for (int J : {128, 256, 384, 512, 768, 1024, 2048, 4096}) {
+                if (J > 128 && J >= maxN + 128) break;
+                e->set_nonbond_chunk(J);
+                const float ms = time_it([&] { launch_nonbond(e->nonbond_args(), e->stream); });
+                if (ms < bestn) {
+                    bestn = ms;
+                    bestJ = J;
+                }
+            }
+            e->set_nonbond_chunk(bestJ);
         }
         // step integrator (unless fixed by the options): the separate bonded,
         // umbrella and leapfrog kernels against the fused cooperative kernel,

@@ -15,6 +15,7 @@
 //  leapfrog: consumes and clears the fixed-point force accumulator, Andersen
 //            collisions from Philox, leapfrog update and wrap
 //            (leapfrog_cuda.cu:33-68).
+#include <algorithm>
 #include <climits>
 #include <cuda_runtime.h>
 
@@ -26,8 +27,21 @@ namespace isspa {
 namespace {
 
 constexpr int kNbThreads = 128;
+constexpr int kNbMaxAB = 4096;  // LJ type pairs held in shared memory (up to 64 LJ types)
 
-__global__ void __launch_bounds__(kNbThreads) nonbond_kernel(NonbondArgs a) {
+// One work item: 128 receiving atoms i (one per thread) against nj partners j
+// starting at item.w, streamed through shared memory in stages of 128.  The
+// per-stage FP32 sums are folded into fixed point per stage, and stages start
+// at multiples of 128 partners from the window's first atom whatever the item
+// length, so the forces do not depend on the partners per item (an autotuned
+// shape).  Exclusions and the self pair are found per stage as a 128-bit mask
+// from the atom's sorted exclusion list; a group of 32 partners that no lane
+// of the warp excludes runs without per-pair checks.  SMEM_AB: the LJ (A, B)
+// table of every ordered type pair sits in shared memory (dynamic, nt^2
+// float2) instead of a global gather per pair.  ALL: every term on (mask 7).
+template <bool SMEM_AB, bool ALL>
+__global__ void __launch_bounds__(kNbThreads, 8) nonbond_kernel(NonbondArgs a) {
+    extern __shared__ float2 s_ab[];
     __shared__ float4 s_x[kNbThreads];
     __shared__ float4 s_c[kNbThreads];  // rmax_j, (2 rmax_j)^2, 8 rmax_j, (1-1/ep)/(24 rmax_j^4)
     __shared__ int s_t[kNbThreads];
@@ -38,25 +52,41 @@ __global__ void __launch_bounds__(kNbThreads) nonbond_kernel(NonbondArgs a) {
     const bool active = t < item.z;
     const int i = item.y + (active ? t : 0);
     const float4 xi = a.pos[i];
-    const int trow = a.atype[i].x * a.n_lj_types;
+    const int nt = a.n_lj_types;
+    const int trow = a.atype[i].x * nt;
     const float L = W.box, h = W.hbox;
-    const int terms = a.terms;
+    const int terms = ALL ? 7 : a.terms;
     const float epf = 1.0f - 1.0f / kEp;
     const float kfar = -2.0f * epf / 3.0f;
+    if (SMEM_AB)
+        for (int k = t; k < nt * nt; k += kNbThreads) s_ab[k] = a.ljab[k];
 
     // exclusion cursor: first entry >= first partner of this item
     int cur = a.excl_start[i];
     const int end = a.excl_start[i + 1];
     while (cur < end && a.excl[cur] < item.w) ++cur;
-    int next_ex = cur < end ? a.excl[cur] : INT_MAX;
 
     long long fxa = 0, fya = 0, fza = 0;  // per-stage partial sums in fixed point
     for (int j0 = 0; j0 < nj; j0 += kNbThreads) {
         const int jn = min(kNbThreads, nj - j0);
+        const int jb = item.w + j0;  // first partner of the stage
+        // exclusion / self bits of this stage's 128 partners
+        unsigned m[4] = {0u, 0u, 0u, 0u};  // register-resident: constant indices only
+        auto set_bit = [&](int b) {
+            const unsigned bit = 1u << (b & 31);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) m[q] |= (b >> 5) == q ? bit : 0u;
+        };
+        for (; cur < end; ++cur) {
+            const int b = a.excl[cur] - jb;
+            if (b >= kNbThreads) break;
+            set_bit(b);
+        }
+        if (i - jb >= 0 && i - jb < kNbThreads) set_bit(i - jb);
         float ax = 0.f, ay = 0.f, az = 0.f;
         __syncthreads();
         if (t < jn) {
-            const int j = item.w + j0 + t;
+            const int j = jb + t;
             s_x[t] = a.pos[j];
             const int2 ty = a.atype[j];
             const float rm = __ldg(a.rmax + ty.y);
@@ -66,14 +96,8 @@ __global__ void __launch_bounds__(kNbThreads) nonbond_kernel(NonbondArgs a) {
             s_t[t] = ty.x;
         }
         __syncthreads();
-        for (int k = 0; k < jn; ++k) {
-            const int j = item.w + j0 + k;
-            const bool ex = j == next_ex;
-            if (ex) {
-                ++cur;
-                next_ex = cur < end ? a.excl[cur] : INT_MAX;
-            }
-            if (j == i) continue;
+        // the pair (i, staged partner k); EX: excluded (IS-SPA correction only)
+        auto pair = [&](int k, bool ex) {
             const float4 xj = s_x[k];
             const float rx = mimg(xi.x - xj.x, L, h);
             const float ry = mimg(xi.y - xj.y, L, h);
@@ -89,7 +113,7 @@ __global__ void __launch_bounds__(kNbThreads) nonbond_kernel(NonbondArgs a) {
             }
             if (!ex) {
                 if (terms & 1) {  // LJ (:131-132)
-                    const float2 ab = __ldg(a.ljab + trow + s_t[k]);
+                    const float2 ab = SMEM_AB ? s_ab[trow + s_t[k]] : __ldg(a.ljab + trow + s_t[k]);
                     const float r6 = ri2 * ri2 * ri2;
                     fs += r6 * fmaf(12.0f * ab.x, r6, -6.0f * ab.y) * ri2;
                 }
@@ -98,6 +122,27 @@ __global__ void __launch_bounds__(kNbThreads) nonbond_kernel(NonbondArgs a) {
             ax = fmaf(fs, rx, ax);
             ay = fmaf(fs, ry, ay);
             az = fmaf(fs, rz, az);
+        };
+#pragma unroll
+        for (int q = 0; q < kNbThreads / 32; ++q) {
+            const int k0 = 32 * q;
+            if (k0 >= jn) break;
+            const int kn = min(32, jn - k0);
+            const unsigned mq = m[q];
+            if (__any_sync(0xffffffffu, mq != 0u)) {
+#pragma unroll 1
+                for (int k = 0; k < kn; ++k) {
+                    const bool bit = (mq >> k) & 1u;
+                    if (bit && jb + k0 + k == i) continue;
+                    pair(k0 + k, bit);
+                }
+            } else if (kn == 32) {
+#pragma unroll 8
+                for (int k = 0; k < 32; ++k) pair(k0 + k, false);
+            } else {
+#pragma unroll 1
+                for (int k = 0; k < kn; ++k) pair(k0 + k, false);
+            }
         }
         if (active) check_force(a.status, ax, ay, az);
         fxa += to_fix(ax);
@@ -144,6 +189,51 @@ __device__ __forceinline__ F3 crossf(F3 a, F3 b) {
 }
 __device__ __forceinline__ F3 scalef(float s, F3 a) { return F3{s * a.x, s * a.y, s * a.z}; }
 
+// Double-float values (hi + lo, two FP32 words) from the error-free
+// transformations of Knuth (TwoSum) and Dekker (TwoProduct, here with an FMA):
+// the bond stretch r0 - |r| and the angle bend theta - theta0 of a geometry
+// near its minimum are small differences of O(1) quantities, which FP32 alone
+// resolves only to ~1e-7 absolute (a relative error of the force that grows
+// as the force vanishes).  Carried in double-float they keep ~1e-7 of their
+// own size; every operation is an FP32 instruction (__fadd_rn / __fmul_rn /
+// fmaf, never contracted or reassociated).
+struct DF {
+    float hi, lo;
+};
+__device__ __forceinline__ DF two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return DF{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ DF fast_two_sum(float a, float b) {  // |a| >= |b|
+    const float s = __fadd_rn(a, b);
+    return DF{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ DF two_prod(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    return DF{p, fmaf(a, b, -p)};
+}
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+    const DF s = two_sum(a.hi, b.hi);
+    return fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ DF df_neg(DF a) { return DF{-a.hi, -a.lo}; }
+__device__ __forceinline__ DF df_mul(DF a, DF b) {
+    const DF p = two_prod(a.hi, b.hi);
+    return fast_two_sum(p.hi, fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, p.lo)));
+}
+// a.b of float vectors, and |a|, in double-float
+__device__ __forceinline__ DF df_dot(F3 a, F3 b) {
+    return df_add(df_add(two_prod(a.x, b.x), two_prod(a.y, b.y)), two_prod(a.z, b.z));
+}
+__device__ __forceinline__ DF df_sqrt(DF a) {  // a > 0; one Newton step on the FP32 root
+    const float s = __fsqrt_rn(a.hi);
+    const float res = __fadd_rn(fmaf(-s, s, a.hi), a.lo);
+    return fast_two_sum(s, __fdiv_rn(res, __fmul_rn(2.0f, s)));
+}
+__device__ __forceinline__ float df_float(DF a) { return __fadd_rn(a.hi, a.lo); }
+
+
 // Fixed-point scatter of one atom's share of a term.
 struct FixAdd {
     unsigned long long *facc;
@@ -165,8 +255,9 @@ __device__ __forceinline__ void bonded_term(const BondedArgs &a, long long idx, 
         const WinDev W = a.win[a.atom_win[b.x]];
         const F3 r = rvec(a.pos, b.x, b.y, W.box, W.hbox);
         const float2 p = a.bond_par[b.z];
-        const float d = __fsqrt_rn(dotf(r, r));
-        const float f = __fdiv_rn(p.x * (p.y - d), d);
+        const DF d = df_sqrt(df_dot(r, r));
+        const float stretch = df_float(df_add(two_sum(p.y, -d.hi), DF{-d.lo, 0.0f}));  // r0 - |r|
+        const float f = __fdiv_rn(__fmul_rn(p.x, stretch), df_float(d));
         add(b.x, scalef(f, r));
         add(b.y, scalef(-f, r));
         return;
@@ -177,12 +268,24 @@ __device__ __forceinline__ void bonded_term(const BondedArgs &a, long long idx, 
         const WinDev W = a.win[a.atom_win[g.x]];
         const F3 r1 = rvec(a.pos, g.x, g.y, W.box, W.hbox);
         const F3 r2 = rvec(a.pos, g.y, g.z, W.box, W.hbox);
-        const F3 w = crossf(r1, r2);
-        const float s = __fsqrt_rn(dotf(w, w));
-        if (!(s > 0.0f)) return;  // collinear: the reference's 1/0
-        const float theta = atan2f(s, -dotf(r1, r2));
+        // |r1 x r2| and r1.r2 in double-float, then theta - theta0 as the angle
+        // of (-r1.r2, |r1 x r2|) rotated by -theta0 (cos and sin of theta0
+        // given in double-float per angle type)
+        const DF wx = df_add(two_prod(r1.y, r2.z), df_neg(two_prod(r1.z, r2.y)));
+        const DF wy = df_add(two_prod(r1.z, r2.x), df_neg(two_prod(r1.x, r2.z)));
+        const DF wz = df_add(two_prod(r1.x, r2.y), df_neg(two_prod(r1.y, r2.x)));
+        const DF s2 = df_add(df_add(df_mul(wx, wx), df_mul(wy, wy)), df_mul(wz, wz));
+        if (!(s2.hi > 0.0f)) return;  // collinear: the reference's 1/0
+        const DF s = df_sqrt(s2);
+        const DF c12 = df_dot(r1, r2);
+        const float4 cs = a.angle_cs[g.w];  // cos theta0 (hi, lo), sin theta0 (hi, lo)
+        const DF ct{cs.x, cs.y}, st{cs.z, cs.w};
+        const float y = df_float(df_add(df_mul(s, ct), df_mul(c12, st)));
+        const float x = fmaf(s.hi, st.hi, -__fmul_rn(c12.hi, ct.hi));
+        const float bend = atan2f(y, x);  // theta - theta0
         const float2 p = a.angle_par[g.w];
-        const float f = __fdiv_rn(p.x * (theta - p.y), s);
+        const F3 w{wx.hi, wy.hi, wz.hi};
+        const float f = __fdiv_rn(__fmul_rn(p.x, bend), df_float(s));
         const F3 fi = scalef(__fdiv_rn(f, dotf(r1, r1)), crossf(r1, w));
         const F3 fk = scalef(__fdiv_rn(f, dotf(r2, r2)), crossf(r2, w));
         add(g.x, fi);
@@ -545,7 +648,28 @@ __global__ void fma_peak_kernel(float *out, int iters, float seed) {
 int nonbond_block_threads() { return kNbThreads; }
 
 void launch_nonbond(const NonbondArgs &a, cudaStream_t s) {
-    if (a.n_items > 0) nonbond_kernel<<<a.n_items, kNbThreads, 0, s>>>(a);
+    if (a.n_items <= 0) return;
+    const int nab = a.n_lj_types * a.n_lj_types;
+    const bool all = a.terms == 7;
+    if (nab <= kNbMaxAB) {
+        const size_t sm = sizeof(float2) * (size_t)std::max(nab, 1);
+        if (all) nonbond_kernel<true, true><<<a.n_items, kNbThreads, sm, s>>>(a);
+        else nonbond_kernel<true, false><<<a.n_items, kNbThreads, sm, s>>>(a);
+    } else {
+        if (all) nonbond_kernel<false, true><<<a.n_items, kNbThreads, 0, s>>>(a);
+        else nonbond_kernel<false, false><<<a.n_items, kNbThreads, 0, s>>>(a);
+    }
+}
+
+int nonbond_blocks_per_sm(int n_lj_types) {
+    int n = 0;
+    const int nab = n_lj_types * n_lj_types;
+    if (nab <= kNbMaxAB)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, nonbond_kernel<true, true>, kNbThreads,
+                                                      sizeof(float2) * (size_t)std::max(nab, 1));
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, nonbond_kernel<false, true>, kNbThreads, 0);
+    return n;
 }
 
 void launch_bonded(const BondedArgs &a, cudaStream_t s) {

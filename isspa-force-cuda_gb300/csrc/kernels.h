@@ -82,6 +82,7 @@ struct BondedArgs {
     const int4 *angles;        // i, j, k, type
     int n_angles;
     const float2 *angle_par;
+    const float4 *angle_cs;    // cos theta0 (hi, lo), sin theta0 (hi, lo): double-float per angle type
     const int4 *dihs;          // i, j, +-k, +-l
     const int *dih_type;
     int n_dihs;
@@ -237,5 +238,6 @@ int nonbond_block_threads();
 int field_points_per_block(int split);
 int field_blocks_per_sm(int split);
 int force_blocks_per_sm(int atoms_per_thread);
+int nonbond_blocks_per_sm(int n_lj_types);
 
 }  // namespace isspa

@@ -51,7 +51,8 @@ class EngineOptions(C.Structure):
     _fields_ = [("isspa_terms", C.c_int), ("nonbond_terms", C.c_int), ("use_graph", C.c_int),
                 ("field_split", C.c_int), ("force_chunk", C.c_int), ("mem_cap", C.c_size_t),
                 ("force_atoms_per_thread", C.c_int), ("force_tail_chunk", C.c_int),
-                ("field_vote", C.c_int), ("force_vote", C.c_int), ("integrator", C.c_int)]
+                ("field_vote", C.c_int), ("force_vote", C.c_int), ("integrator", C.c_int),
+                ("nonbond_chunk", C.c_int)]
 
 
 class RunConfig(C.Structure):

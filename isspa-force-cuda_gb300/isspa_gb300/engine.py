@@ -24,7 +24,8 @@ class Engine:
     def __init__(self, windows: "System | Sequence[System]", isspa_terms: int = 7,
                  nonbond_terms: int = 7, use_graph: bool = True, field_split: int = 0,
                  force_chunk: int = 0, mem_cap: int = 0, force_atoms_per_thread: int = 0,
-                 force_tail_chunk: int = 0, field_vote: int = 0, force_vote: int = 0, integrator: int = 0):
+                 force_tail_chunk: int = 0, field_vote: int = 0, force_vote: int = 0, integrator: int = 0,
+                 nonbond_chunk: int = 0):
         if isinstance(windows, System):
             windows = [windows]
         self.windows = list(windows)
@@ -45,6 +46,7 @@ class Engine:
         opt.field_vote = int(field_vote)
         opt.force_vote = int(force_vote)
         opt.integrator = int(integrator)
+        opt.nonbond_chunk = int(nonbond_chunk)
         h = C.c_void_p()
         abi.check(L.isspa_engine_create(descs, len(self.windows), C.byref(opt), C.byref(h)), "engine create")
         self._h = h

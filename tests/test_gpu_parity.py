@@ -137,6 +137,22 @@ def test_nonbond_medium(synth_medium):
     check_force(eng.forces(), O.Oracle(synth_medium).nonbond(7), "nonbond medium")
 
 
+def test_nonbond_partner_chunks_bit_identical(synth_medium):
+    """Partners per nonbond work item (128..all, ragged last items) move no
+    bit of the force: the per-stage sums start at the same partners."""
+    out = []
+    for chunk in (128, 256, 384, 1024):
+        eng = ig.Engine(synth_medium, nonbond_chunk=chunk)
+        assert eng.shapes()["nonbond_partners_per_item"] == chunk
+        eng.zero_forces()
+        eng.nonbond_force()
+        out.append(eng.forces())
+        eng.close()
+    for f in out[1:]:
+        assert np.array_equal(f, out[0])
+    check_force(out[0], O.Oracle(synth_medium).nonbond(7), "nonbond medium, 128-partner items")
+
+
 @pytest.mark.parametrize("which", ["adi2", "medium"])
 def test_bonded_matches_oracle(which, adi2, synth_medium):
     s = with_mc(adi2, 10) if which == "adi2" else synth_medium
