@@ -135,7 +135,7 @@ def ncu_traffic(kernel: str):
     return d.get(kernel)
 
 
-def force_errors(f, ref, floor=0.05):
+def force_errors(f, ref, floor=0.10):
     """Normwise max |dF| / max |F| and the per-atom |dF_i| / |F_i| (median,
     max) over atoms with |F_i| >= floor x the largest |F|."""
     f = np.asarray(f, np.float64)[:, :3]
@@ -485,6 +485,16 @@ def run_precision(ig, args, peak_fp32):
     steps = 5
     ms = eng.time_steps(steps, L2_FLUSH)
     _, kern = eng.time_steps_detailed(steps, L2_FLUSH)
+    # each pass alone on the GPU (per-call entry points, CUDA events around the
+    # launch): in the step graph the bonded / nonbond branch shares the SMs
+    # with the field pass, so its event interval there is not its own time
+    alone = {}
+    bonded = lambda timed: eng.bond_force(timed) + eng.angle_force(timed) + eng.dih_force(timed)
+    for name, call in (("nonbond", eng.nonbond_force), ("bonded (bond + angle + dihedral calls)", bonded)):
+        eng.zero_forces()
+        call(True)
+        alone[name] = round(min(call(True) for _ in range(3)), 4)
+    eng.zero_forces()
     status = eng.device_status()
     eng.close()
     avg = {k: v[0] / v[1] for k, v in kern.items() if v[1] > 0}
@@ -495,6 +505,9 @@ def run_precision(ig, args, peak_fp32):
             "ms_per_step": round(ms / steps, 3),
             "ns_per_day": round(ns_per_day(steps / (ms * 1e-3)), 2),
             "kernel_ms_per_launch": {k: round(v, 3) for k, v in avg.items()},
+            "kernel_ms_alone": alone,
+            "nonbond_alone_tflops": round(FLOP_NB_PAIR * N * (N - 1) / (alone["nonbond"] * 1e-3) / 1e12, 2),
+            "nonbond_alone_frac": round(FLOP_NB_PAIR * N * (N - 1) / (alone["nonbond"] * 1e-3) / 1e12 / peak_fp32, 4),
             "force_kernel_tflops": round(force_tf, 2), "force_kernel_frac": round(force_tf / peak_fp32, 4),
             "field_kernel_tflops": round(field_tf, 2), "field_kernel_frac": round(field_tf / peak_fp32, 4),
             "launch_shapes": shapes, "device_status": status,

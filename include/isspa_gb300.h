@@ -126,6 +126,9 @@ typedef struct isspa_engine_options {
                             0 => 1 until isspa_autotune times both and keeps the faster */
     int nonbond_chunk;   /* partners per nonbond work item (rounded up to a multiple of 128;
                             the results do not depend on it); 0 => auto */
+    int field_tma;       /* 1: the field pass stages each round of 128 atoms with a 1-D bulk
+                            copy (cp.async.bulk, the TMA engine) behind an mbarrier, double-
+                            buffered (same results); 0 => coalesced loads by the threads */
 } isspa_engine_options;
 
 #define ISSPA_TERMS_NONE (-1)
@@ -189,11 +192,12 @@ int isspa_engine_info(const isspa_engine *e, int *n_windows, int *n_atoms_total,
  * thread, [8] points per force work item of the short items listed last (0:
  * none), [9] 1 when the field pass walks its atoms in warp-voted groups,
  * [10] 1 when the force pass takes its points in warp-voted groups, [11] the
- * step integrator (1 separate kernels, 2 fused; see isspa_engine_options). */
-#define ISSPA_SHAPE_COUNT 12
+ * step integrator (1 separate kernels, 2 fused; see isspa_engine_options),
+ * [12] 1 when the field pass stages its atoms by bulk copies (TMA). */
+#define ISSPA_SHAPE_COUNT 13
 int isspa_engine_shapes(const isspa_engine *e, int shape[ISSPA_SHAPE_COUNT]);
 /* Autotuner: times every field-pass atom split (per-pair and warp-voted
- * loops) and, for 1 and 2 receiving
+ * loops, atoms staged by loads or by bulk copies) and, for 1 and 2 receiving
  * atoms per force thread, a set of force-pass chunk lengths (those filling
  * 1..12 whole waves of resident blocks, and powers of two; and long chunks
  * followed by about two waves of short ones; then the voted force loop on the

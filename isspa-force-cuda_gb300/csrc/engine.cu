@@ -90,6 +90,7 @@ struct isspa_engine {
     int n_force_items = 0, force_chunk = 0;
     int force_tail = 0;  // chunk length of the short items listed last (0: none)
     int field_vote = 0;  // field pass in warp-voted groups of four atoms
+    int field_tma = 0;   // field pass stages its atom rounds by 1-D bulk copies (TMA)
     int force_vote = 0;  // force pass in warp-voted groups of four points (1 atom per thread)
     int force_apt = 1;  // receiving atoms per force-kernel thread (1 or 2)
     // step integrator: 1 = bonded, umbrella and leapfrog kernels (bonded and
@@ -336,6 +337,7 @@ struct isspa_engine {
     FieldArgs field_args() const {
         FieldArgs a{};
         a.vote = field_vote;
+        a.tma = field_tma;
         a.pos = pos;
         a.atype = atype;
         a.win = win;
@@ -853,6 +855,7 @@ void build(isspa_engine &E, const std::vector<isspa_host_system> &ws) {
     if (S != 1 && S != 2 && S != 4 && S != 8 && S != 16) S = E.default_field_split();
     E.set_field_split(S);
     E.field_vote = E.opt.field_vote == 1 ? 1 : 0;
+    E.field_tma = E.opt.field_tma == 1 ? 1 : 0;
     E.force_vote = E.opt.force_vote == 1 ? 1 : 0;
     E.force_apt = E.opt.force_atoms_per_thread == 2 ? 2 : 1;
     E.set_force_chunk(E.opt.force_chunk > 0 ? E.opt.force_chunk : E.default_force_chunk(),
@@ -1093,6 +1096,7 @@ int isspa_engine_shapes(const isspa_engine *e, int shape[ISSPA_SHAPE_COUNT]) {
     shape[9] = e->field_vote;
     shape[10] = e->force_apt == 1 ? e->force_vote : 0;
     shape[11] = e->integrator;
+    shape[12] = e->field_tma;
     return ISSPA_OK;
 }
 
@@ -1340,22 +1344,27 @@ int isspa_autotune(isspa_engine *e, int reps, int shape[ISSPA_SHAPE_COUNT]) {
             ck(cudaEventElapsedTime(&ms, e->ev_a, e->ev_b));
             return ms / reps;
         };
-        // field pass: every atom-loop split, per-pair and warp-voted loops
+        // field pass: every atom-loop split, per-pair and warp-voted loops,
+        // atom rounds staged by plain loads and by bulk copies (TMA)
         float best = 1e30f;
-        int bestS = e->field_split, bestV = e->field_vote;
-        for (int V : {0, 1})
-            for (int S : {1, 2, 4, 8, 16}) {
-                e->set_field_split(S);
-                e->field_vote = V;
-                const float ms = time_it([&] { launch_field(e->field_args(), S, false, e->stream); });
-                if (ms < best) {
-                    best = ms;
-                    bestS = S;
-                    bestV = V;
+        int bestS = e->field_split, bestV = e->field_vote, bestTma = e->field_tma;
+        for (int T : {0, 1})
+            for (int V : {0, 1})
+                for (int S : {1, 2, 4, 8, 16}) {
+                    e->set_field_split(S);
+                    e->field_vote = V;
+                    e->field_tma = T;
+                    const float ms = time_it([&] { launch_field(e->field_args(), S, false, e->stream); });
+                    if (ms < best) {
+                        best = ms;
+                        bestS = S;
+                        bestV = V;
+                        bestTma = T;
+                    }
                 }
-            }
         e->set_field_split(bestS);
         e->field_vote = bestV;
+        e->field_tma = bestTma;
         launch_field(e->field_args(), bestS, false, e->stream);
         // force pass: for 1 and 2 atoms per thread, the chunk lengths that fill
         // 1..12 whole waves of that kernel's resident blocks, and powers of two

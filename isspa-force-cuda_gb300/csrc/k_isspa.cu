@@ -81,6 +81,37 @@ __device__ __forceinline__ void mc_point(uint32_t p, uint32_t window, uint32_t s
     pz = __fmaf_rn(mz, rm, xa.z);
 }
 
+// 1-D bulk copies (cp.async.bulk, the TMA engine's untiled form) from global
+// into this CTA's shared memory, completed on an mbarrier; every wait is
+// bounded.  Both addresses are 16-byte aligned and sizes multiples of 16.
+__device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long *bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_init_fence() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void proxy_fence() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, unsigned bytes, unsigned long long *bar) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+// Waits for phase `parity` of the barrier; false after kBulkSpins polls.
+constexpr int kBulkSpins = 1 << 22;
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity) {
+    for (int it = 0; it < kBulkSpins; ++it) {
+        unsigned done;
+        asm volatile(
+            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+            : "=r"(done)
+            : "r"(smem_addr(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
 // Block shape of the field kernel: S warps split the atom loop of each group
 // of 32 points; 4 warps per block up to S = 4, then 32*S threads.
 template <int S>
@@ -90,17 +121,24 @@ struct FieldShape {
 
 // VOTE: the atom loop takes groups of four atoms and one warp vote per group
 // (see below); same operations in the same order as the per-pair loop.
-template <int S, bool GEN, bool RAW, bool VOTE>
+// TMA: the window's atoms arrive in rounds of 128 by 1-D bulk copies of the
+// position array, double-buffered behind two mbarriers (thread 0 issues round
+// r + 2 as soon as round r has been read); e0 q and the table row are formed
+// at use (the same products, so the same results).  One warp vote per round
+// makes a bounded wait that gave up block-uniform: the block then flags
+// kStatusTimeout, waits (bounded) for its copies still in flight and exits.
+template <int S, bool GEN, bool RAW, bool VOTE, bool TMA = false>
 __global__ void __launch_bounds__(FieldShape<S>::kThreads) field_kernel(FieldArgs a) {
     constexpr int kT = FieldShape<S>::kThreads;
     // atoms staged per round: four per thread below a split of 4, so the
     // warps' compute phases between barriers are four times longer (64 windows
     // at split 1: 1.779 against 1.808 ms per launch; at split 8 one per thread
     // measured faster); a multiple of S either way, so each warp still visits
-    // its atoms (j = sp mod S) in increasing order
-    constexpr int kA = S >= 4 ? kT : 4 * kT;
-    __shared__ float4 s_atom[kA];
-    __shared__ int s_row[kA];
+    // its atoms (j = sp mod S) in increasing order, whatever the round length
+    constexpr int kA = TMA ? 128 : (S >= 4 ? kT : 4 * kT);
+    __shared__ alignas(16) float4 s_atom[TMA ? 2 : 1][kA];
+    __shared__ int s_row[TMA ? 1 : kA];
+    __shared__ alignas(8) unsigned long long s_bar[2];
     __shared__ float s_red[S > 1 ? 8 : 1][kT];
     constexpr bool kShareDraws = GEN && S >= 4;
     __shared__ float s_pt[3][kShareDraws ? kT / S : 1];  // the block's points, drawn once
@@ -120,13 +158,14 @@ __global__ void __launch_bounds__(FieldShape<S>::kThreads) field_kernel(FieldArg
     const float L = W.box, h = W.hbox;
 
     const int nb = a.n_gbins;
+    const int n_rounds = (W.n_atoms + kA - 1) / kA;
     // one round of the window's atoms into shared memory: [j0, j0 + jn)
     auto stage_round = [&](int j0, int jn) {
         auto stage = [&](int i) {
             const int j = W.atom_off + j0 + i;
             float4 xj = a.pos[j];
             xj.w = a.e0 * xj.w;  // e0*q (isspa_force_cuda.cu:179, :183)
-            s_atom[i] = xj;
+            s_atom[0][i] = xj;
             s_row[i] = a.atype[j].y * nb;
         };
         if (kA == kT) {
@@ -136,9 +175,23 @@ __global__ void __launch_bounds__(FieldShape<S>::kThreads) field_kernel(FieldArg
             for (int i = threadIdx.x; i < jn; i += kT) stage(i);
         }
     };
-    // the first round is staged before the points are known, so its loads
-    // overlap the draws and the barrier below covers both
-    stage_round(0, min(kA, W.n_atoms));
+    auto issue_round = [&](int r) {  // TMA, thread 0
+        const int jn = min(kA, W.n_atoms - r * kA);
+        bulk_load(s_atom[r & 1], a.pos + W.atom_off + r * kA, 16u * (unsigned)jn, &s_bar[r & 1]);
+    };
+    // the first round is staged (or issued) before the points are known, so
+    // its loads overlap the draws and the barrier below covers both
+    if (TMA) {
+        if (threadIdx.x == 0) {
+            mbar_init(&s_bar[0]);
+            mbar_init(&s_bar[1]);
+            mbar_init_fence();
+            issue_round(0);
+            if (n_rounds > 1) issue_round(1);
+        }
+    } else {
+        stage_round(0, min(kA, W.n_atoms));
+    }
 
     float px, py, pz;
     if (kShareDraws) {
@@ -179,14 +232,15 @@ __global__ void __launch_bounds__(FieldShape<S>::kThreads) field_kernel(FieldArg
 
     // geometry of the pair (point, staged atom k); true when inside rmax of
     // the owner's type (:154)
+    int buf = 0, jbase = 0;  // staged buffer and first atom of the current round
     auto geom = [&](int k, float &rx, float &ry, float &rz, float &c) {
-        const float4 xj = s_atom[k];
+        const float4 xj = s_atom[TMA ? buf : 0][k];
         rx = mimg(px - xj.x, L, h);
         ry = mimg(py - xj.y, L, h);
         rz = mimg(pz - xj.z, L, h);
         const float d2 = dist2f(rx, ry, rz);
         const float ri = rsqrtf(d2);
-        c = xj.w * (ri * ri * ri);
+        c = (TMA ? a.e0 * xj.w : xj.w) * (ri * ri * ri);
         return d2 <= rm2;
     };
     // ex.. accumulates the in-range contributions (Coulomb and tabulated
@@ -206,7 +260,8 @@ __global__ void __launch_bounds__(FieldShape<S>::kThreads) field_kernel(FieldArg
             if (bin < 0) {
                 w = 0.0f;
             } else if (bin < nb) {
-                const float4 t = __ldg(a.gtab + s_row[k] + bin);
+                const int row = TMA ? __ldg(&a.atype[W.atom_off + jbase + k].y) * nb : s_row[k];
+                const float4 t = __ldg(a.gtab + row + bin);
                 const float fg = (dist - fmaf((float)bin, g_dr, g_r0)) * g_inv;
                 w *= fmaf(fg, t.y - t.x, t.x);
                 const float fe = (dist - fmaf((float)bin, e_dr, e_r0)) * e_inv;
@@ -222,9 +277,26 @@ __global__ void __launch_bounds__(FieldShape<S>::kThreads) field_kernel(FieldArg
         }
     };
 
-    for (int j0 = 0; j0 < W.n_atoms; j0 += kA) {
+    for (int j0 = 0, r = 0; j0 < W.n_atoms; j0 += kA, ++r) {
         const int jn = min(kA, W.n_atoms - j0);
-        if (j0 > 0) {
+        if (TMA) {
+            buf = r & 1;
+            jbase = j0;
+            if (r > 0) {
+                __syncthreads();  // round r - 1 has been read: its buffer takes round r + 1
+                if (threadIdx.x == 0 && r + 1 < n_rounds) {
+                    proxy_fence();
+                    issue_round(r + 1);
+                }
+            }
+            if (!__syncthreads_and(mbar_wait(&s_bar[buf], (unsigned)(r >> 1) & 1u))) {
+                if (threadIdx.x == 0) {
+                    atomicOr(a.status, kStatusTimeout);
+                    for (int q = r; q < min(r + 2, n_rounds); ++q) mbar_wait(&s_bar[q & 1], (unsigned)(q >> 1) & 1u);
+                }
+                return;
+            }
+        } else if (j0 > 0) {
             __syncthreads();  // the previous round has been read
             stage_round(j0, jn);
             __syncthreads();
@@ -497,17 +569,20 @@ __global__ void __launch_bounds__(ForceShape<A>::kThreads, VOTE ? 8 : ForceShape
     }
 }
 
-template <int S, bool GEN, bool RAW, bool VOTE = false>
+template <int S, bool GEN, bool RAW, bool VOTE = false, bool TMA = false>
 void launch_field_t(const FieldArgs &a, cudaStream_t s) {
-    field_kernel<S, GEN, RAW, VOTE><<<a.n_tiles, FieldShape<S>::kThreads, 0, s>>>(a);
+    field_kernel<S, GEN, RAW, VOTE, TMA><<<a.n_tiles, FieldShape<S>::kThreads, 0, s>>>(a);
 }
 
 template <int S>
 void launch_field_s(const FieldArgs &a, bool raw, cudaStream_t s) {
     const bool gen = a.pts_in == nullptr;
-    // the vote variant gives the same results; the raw-field captures (tests,
-    // adjoint) always take the per-pair loop
-    if (a.vote && !raw) {
+    // the vote and TMA variants give the same results; the raw-field captures
+    // (tests, adjoint) always take the per-pair loop with plain staging
+    if (a.tma && gen && !raw) {
+        if (a.vote) launch_field_t<S, true, false, true, true>(a, s);
+        else launch_field_t<S, true, false, false, true>(a, s);
+    } else if (a.vote && !raw) {
         if (gen) launch_field_t<S, true, false, true>(a, s);
         else launch_field_t<S, false, false, true>(a, s);
     } else if (gen && !raw) launch_field_t<S, true, false>(a, s);

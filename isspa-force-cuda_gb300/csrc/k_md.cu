@@ -61,10 +61,15 @@ __global__ void __launch_bounds__(kNbThreads, 8) nonbond_kernel(NonbondArgs a) {
     if (SMEM_AB)
         for (int k = t; k < nt * nt; k += kNbThreads) s_ab[k] = a.ljab[k];
 
-    // exclusion cursor: first entry >= first partner of this item
-    int cur = a.excl_start[i];
+    // exclusion cursor: first entry >= first partner of this item; the list
+    // is sorted, so an item outside [first, last] entry needs no walk
     const int end = a.excl_start[i + 1];
-    while (cur < end && a.excl[cur] < item.w) ++cur;
+    int cur = a.excl_start[i];
+    if (cur < end) {
+        if (a.excl[end - 1] < item.w || a.excl[cur] >= item.w + nj) cur = end;
+        else
+            while (cur < end && a.excl[cur] < item.w) ++cur;
+    }
 
     long long fxa = 0, fya = 0, fza = 0;  // per-stage partial sums in fixed point
     for (int j0 = 0; j0 < nj; j0 += kNbThreads) {
@@ -79,7 +84,7 @@ __global__ void __launch_bounds__(kNbThreads, 8) nonbond_kernel(NonbondArgs a) {
         };
         for (; cur < end; ++cur) {
             const int b = a.excl[cur] - jb;
-            if (b >= kNbThreads) break;
+            if (b >= kNbThreads || j0 + b >= nj) break;
             set_bit(b);
         }
         if (i - jb >= 0 && i - jb < kNbThreads) set_bit(i - jb);

@@ -29,6 +29,7 @@ struct FieldArgs {
     int terms;             // IS-SPA force terms: 1 multipole, 2 tabulated LJ, 4 CDD
     int *status;
     int vote;              // 1: atom loop in warp-voted groups of four (same results)
+    int tma;               // 1: atom rounds staged by 1-D bulk copies (TMA) behind mbarriers (same results)
 };
 
 // ---- IS-SPA force pass (one thread per receiving atom) -------------------

@@ -25,7 +25,7 @@ class Engine:
                  nonbond_terms: int = 7, use_graph: bool = True, field_split: int = 0,
                  force_chunk: int = 0, mem_cap: int = 0, force_atoms_per_thread: int = 0,
                  force_tail_chunk: int = 0, field_vote: int = 0, force_vote: int = 0, integrator: int = 0,
-                 nonbond_chunk: int = 0):
+                 nonbond_chunk: int = 0, field_tma: int = 0):
         if isinstance(windows, System):
             windows = [windows]
         self.windows = list(windows)
@@ -47,6 +47,7 @@ class Engine:
         opt.force_vote = int(force_vote)
         opt.integrator = int(integrator)
         opt.nonbond_chunk = int(nonbond_chunk)
+        opt.field_tma = int(field_tma)
         h = C.c_void_p()
         abi.check(L.isspa_engine_create(descs, len(self.windows), C.byref(opt), C.byref(h)), "engine create")
         self._h = h
@@ -60,7 +61,7 @@ class Engine:
         abi.check(abi.lib().isspa_engine_shapes(self._h, v), "shapes")
         keys = ("field_split", "field_tiles", "force_chunk", "force_items", "nonbond_items",
                 "nonbond_partners_per_item", "sms", "force_atoms_per_thread", "force_tail_chunk",
-                "field_vote", "force_vote", "integrator")
+                "field_vote", "force_vote", "integrator", "field_tma")
         return dict(zip(keys, list(v)))
 
     def autotune(self, reps: int = 3) -> dict:

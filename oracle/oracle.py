@@ -336,6 +336,13 @@ def philox(ctr, key):
     return list(out)
 
 
+def set_langevin_float_closed_forms(on: bool) -> None:
+    """Diagnostic: evaluate <P1>, <P2>, <P3> with the reference's float closed
+    forms (isspa_force_cuda.cu:270-287) instead of the accurate evaluation
+    (process-wide until switched back)."""
+    lib().orc_set_langevin_mode(1 if on else 0)
+
+
 def langevin(x: float):
     out = (C.c_double * 3)()
     lib().orc_langevin(C.c_double(x), out)

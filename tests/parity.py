@@ -12,7 +12,7 @@ import numpy as np
 
 FORCE_TOL = 1e-5        # normwise, the 1e-5 relative target
 PER_ATOM_TOL = 1e-5     # per atom, above the floor
-PER_ATOM_FLOOR = 0.05   # fraction of the largest force magnitude
+PER_ATOM_FLOOR = 0.10   # fraction of the largest force magnitude
 
 
 def nrel(a, b):

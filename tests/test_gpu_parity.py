@@ -68,19 +68,39 @@ def test_mc_points_bit_identical(adi2_100):
 
 @pytest.mark.parametrize("split", [1, 2, 4, 8, 16])
 def test_field_vote_loop_bit_identical(synth_medium, split):
-    """The warp-voted atom loop of the field pass gives the per-pair loop's
-    forces and trajectory bit for bit, at every atom-loop split."""
+    """The warp-voted atom loop of the field pass, and atom rounds staged by
+    bulk copies (TMA) instead of thread loads, give the per-pair loop's forces
+    and trajectory bit for bit, at every atom-loop split."""
     out = []
-    for vote in (0, 1):
-        eng = ig.Engine(synth_medium, field_split=split, field_vote=vote)
-        assert eng.shapes()["field_vote"] == vote and eng.shapes()["field_split"] == split
+    for vote, tma in ((0, 0), (1, 0), (0, 1), (1, 1)):
+        eng = ig.Engine(synth_medium, field_split=split, field_vote=vote, field_tma=tma)
+        sh = eng.shapes()
+        assert sh["field_vote"] == vote and sh["field_split"] == split and sh["field_tma"] == tma
+        eng.zero_forces()
+        eng.isspa_force()
+        f = eng.forces()
+        eng.step(5)
+        out.append((f, eng.positions()))
+        assert eng.device_status() == 0
+    for f, p in out[1:]:
+        assert np.array_equal(f, out[0][0])
+        assert np.array_equal(p, out[0][1])
+
+
+def test_field_tma_batched_windows_bit_identical():
+    """Bulk-copied atom rounds over windows of odd sizes and odd first atoms
+    (1, 2, 44, 23 and 1100 atoms) give the plain staging's forces bit for bit."""
+    ff = ig.synth.forcefield(n_mc=20)
+    wins = [ig.synth.make_system(c, ln, 40.0, 20, seed=40 + k, ff=ff)
+            for k, (c, ln) in enumerate([(1, 1), (2, 1), (2, 22), (1, 23), (50, 22)])]
+    out = []
+    for tma in (0, 1):
+        eng = ig.Engine(wins, field_tma=tma)
         eng.zero_forces()
         eng.isspa_force()
         out.append(eng.forces())
-        eng.step(5)
-        out.append(eng.positions())
-    assert np.array_equal(out[0], out[2])
-    assert np.array_equal(out[1], out[3])
+        assert eng.device_status() == 0
+    assert np.array_equal(out[0], out[1])
 
 
 @pytest.mark.parametrize("which", ["adi2", "medium", "medium-two-grids"])

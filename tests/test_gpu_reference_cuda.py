@@ -57,8 +57,14 @@ def test_isspa_force_same_points_as_reference_cuda(ref_cuda, adi2, which):
     eng.isspa_force()
     f = eng.forces()
     orc = o.isspa_force(pts)
+    O.set_langevin_float_closed_forms(True)
+    try:
+        orc_closed = o.isspa_force(pts)
+    finally:
+        O.set_langevin_float_closed_forms(False)
     rows = {"engine vs reference CUDA": (f, ref), "reference CUDA vs FP64 oracle": (ref, orc),
-            "engine vs FP64 oracle": (f, orc)}
+            "engine vs FP64 oracle": (f, orc),
+            "reference CUDA vs FP64 oracle with the reference's float Langevin closed forms": (ref, orc_closed)}
     print(f"{which}: reference run-to-run spread (normwise) {spread:.2e}")
     for name, (a, b) in rows.items():
         med, mx, k, tot = per_atom(a, b)
