@@ -97,19 +97,27 @@ __device__ __forceinline__ void bulk_load(void *dst, const void *src, unsigned b
                  "l"(src), "r"(bytes), "r"(smem_addr(bar))
                  : "memory");
 }
-// Waits for phase `parity` of the barrier; false after kBulkSpins polls.
-constexpr int kBulkSpins = 1 << 22;
+// Waits for phase `parity` of the barrier with non-blocking polls; false once
+// kBulkWaitNs of global time have passed (a deadline in time, not in polls).
+constexpr unsigned long long kBulkWaitNs = 1000000000ull;
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity) {
-    for (int it = 0; it < kBulkSpins; ++it) {
+    const unsigned long long t0 = global_ns();
+    for (;;) {
         unsigned done;
         asm volatile(
-            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+            "{ .reg .pred p; mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
             : "=r"(done)
             : "r"(smem_addr(bar)), "r"(parity)
             : "memory");
         if (done) return true;
+        if (global_ns() - t0 > kBulkWaitNs) return false;
+        __nanosleep(32);
     }
-    return false;
 }
 
 // Block shape of the field kernel: S warps split the atom loop of each group

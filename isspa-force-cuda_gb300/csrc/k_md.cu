@@ -506,9 +506,14 @@ __device__ __forceinline__ void leapfrog_atom(const LeapfrogArgs &a, int i, uint
 
 // Grid-wide barrier of a cooperative launch (every block resident): arrival
 // count and generation word, both zero at rest.  The wait is bounded: after
-// kBarrierSpins polls the block gives up, flags kStatusTimeout and returns
-// false, and the caller skips the work that needed the barrier.
-constexpr long long kBarrierSpins = 1LL << 22;
+// kBarrierWaitNs of global time the block gives up, flags kStatusTimeout and
+// returns false, and the caller skips the work that needed the barrier.
+constexpr unsigned long long kBarrierWaitNs = 500000000ull;
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 __device__ bool grid_barrier(unsigned int *bar, int *status) {
     __shared__ int s_ok;
     __syncthreads();
@@ -522,9 +527,9 @@ __device__ bool grid_barrier(unsigned int *bar, int *status) {
             __threadfence();
             atomicAdd(bar + 1, 1u);
         } else {
-            long long spins = 0;
+            const unsigned long long t0 = global_ns();
             while (*gen == g) {
-                if (++spins > kBarrierSpins) {
+                if (global_ns() - t0 > kBarrierWaitNs) {
                     atomicOr(status, kStatusTimeout);
                     ok = 0;
                     break;

@@ -13,16 +13,17 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(os.path.dirname(HERE), "ref_omp"))
 
 
-def harness() -> str:
+def harness(fast_math: bool = True) -> str:
     import build_ref
 
-    return build_ref.build_cuda()
+    return build_ref.build_cuda(fast_math)
 
 
-def forces(system, pts, runs: int = 5) -> np.ndarray:
+def forces(system, pts, runs: int = 5, fast_math: bool = True) -> np.ndarray:
     """IS-SPA force of every atom ([runs][N][3]) from the reference kernels on
     the points `pts` ([N*nMC][3]); each run starts from zeroed accumulators
-    (the reference's float atomics make runs differ at rounding level)."""
+    (the reference's float atomics make runs differ at rounding level).
+    fast_math=False uses the build without -use_fast_math."""
     s = system
     n, m = int(s.n_atoms), int(s.n_mc)
     nt = len(s.rmax)
@@ -39,7 +40,7 @@ def forces(system, pts, runs: int = 5) -> np.ndarray:
                       np.ascontiguousarray(s.vtot(), np.float32), g, e, f,
                       np.ascontiguousarray(pts, np.float32).reshape(n * m, 3)):
                 fh.write(a.tobytes())
-        r = subprocess.run([harness(), fin, fout], capture_output=True, text=True, timeout=600)
+        r = subprocess.run([harness(fast_math), fin, fout], capture_output=True, text=True, timeout=600)
         if r.returncode != 0:
             raise RuntimeError(f"reference harness exited {r.returncode}: {r.stderr.strip()}")
         out = np.fromfile(fout, np.float32).reshape(runs, n, 4)

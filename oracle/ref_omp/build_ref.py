@@ -82,24 +82,29 @@ def build() -> str:
     return LIB
 
 
-def build_cuda() -> str:
-    """The reference CUDA harness; raises when the staged sources or nvcc are missing."""
+def build_cuda(fast_math: bool = True) -> str:
+    """The reference CUDA harness, with the reference's -use_fast_math (as its
+    Makefile builds) or without it (IEEE division, square root and tanh: a
+    diagnostic of what the flag contributes); raises when the staged sources
+    or nvcc are missing."""
     stage()
     for name in CUDA_FILES:
         if not os.path.exists(os.path.join(SRC_DIR, name)):
             raise FileNotFoundError("reference CUDA source not staged: src/" + name)
+    out = HARNESS if fast_math else HARNESS + "_ieee"
     deps = [HARNESS_SRC] + [os.path.join(SRC_DIR, n) for n in CUDA_FILES]
-    if os.path.exists(HARNESS) and all(os.path.getmtime(HARNESS) >= os.path.getmtime(d) for d in deps):
-        return HARNESS
+    if os.path.exists(out) and all(os.path.getmtime(out) >= os.path.getmtime(d) for d in deps):
+        return out
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
-    tmp = HARNESS + ".tmp"
-    subprocess.check_call([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-use_fast_math", "-lineinfo",
-                           "-Wno-deprecated-gpu-targets", "-Wno-deprecated-declarations", "-I", SRC_DIR,
-                           "-o", tmp, HARNESS_SRC])
-    os.replace(tmp, HARNESS)
-    return HARNESS
+    tmp = out + ".tmp"
+    subprocess.check_call([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo",
+                           "-Wno-deprecated-gpu-targets", "-Wno-deprecated-declarations", "-I", SRC_DIR]
+                          + (["-use_fast_math"] if fast_math else []) + ["-o", tmp, HARNESS_SRC])
+    os.replace(tmp, out)
+    return out
 
 
 if __name__ == "__main__":
     print(build())
     print(build_cuda())
+    print(build_cuda(fast_math=False))
