@@ -119,11 +119,16 @@ typedef struct isspa_engine_options {
     int force_vote;      /* 1: the force pass (one atom per thread) takes its points in
                             groups of four with one warp vote per group (same results);
                             0 => per-pair branches */
-    int integrator;      /* step integrator of isspa_step: 1 = bonded, umbrella and leapfrog
+    int integrator;      /* how isspa_step runs a step: 1 = bonded, umbrella and leapfrog
                             kernels (bonded and umbrella concurrent with the IS-SPA pass);
                             2 = one fused cooperative kernel for bonded, umbrella and
-                            leapfrog after the force passes (same results bit for bit);
-                            0 => 1 until isspa_autotune times both and keeps the faster */
+                            leapfrog after the force passes; 3 = the whole step in one
+                            cooperative kernel (field, nonbond, bonded | force | update,
+                            with grid barriers; for latency-bound small systems; takes the
+                            field split 4, and needs the tabulated LJ term, Philox points,
+                            one receiving atom per force thread and at most 64 LJ types,
+                            else 1).  Same results bit for bit for the same launch shapes;
+                            0 => 1 until isspa_autotune times them all and keeps the fastest */
     int nonbond_chunk;   /* partners per nonbond work item (rounded up to a multiple of 128;
                             the results do not depend on it); 0 => auto */
     int field_tma;       /* 1: the field pass stages each round of 128 atoms with a 1-D bulk
@@ -192,7 +197,7 @@ int isspa_engine_info(const isspa_engine *e, int *n_windows, int *n_atoms_total,
  * thread, [8] points per force work item of the short items listed last (0:
  * none), [9] 1 when the field pass walks its atoms in warp-voted groups,
  * [10] 1 when the force pass takes its points in warp-voted groups, [11] the
- * step integrator (1 separate kernels, 2 fused; see isspa_engine_options),
+ * step integrator (1 separate kernels, 2 fused, 3 single-kernel step; see isspa_engine_options),
  * [12] 1 when the field pass stages its atoms by bulk copies (TMA). */
 #define ISSPA_SHAPE_COUNT 13
 int isspa_engine_shapes(const isspa_engine *e, int shape[ISSPA_SHAPE_COUNT]);
@@ -237,7 +242,7 @@ int isspa_time_steps(isspa_engine *e, int nsteps, size_t flush_bytes, double *ms
  * ms_kernels[ISSPA_K_COUNT] receives the summed milliseconds per kernel and
  * launches[ISSPA_K_COUNT] the number of launches of each. */
 enum { ISSPA_K_FIELD = 0, ISSPA_K_FORCE, ISSPA_K_NONBOND, ISSPA_K_BONDED, ISSPA_K_UMBRELLA,
-       ISSPA_K_LEAPFROG, ISSPA_K_INTEGRATOR, ISSPA_K_COUNT };
+       ISSPA_K_LEAPFROG, ISSPA_K_INTEGRATOR, ISSPA_K_STEP, ISSPA_K_COUNT };
 int isspa_time_steps_detailed(isspa_engine *e, int nsteps, size_t flush_bytes, double *ms_total,
                               double *ms_kernels, int *launches);
 /* Page-locked host buffers, mapped into the device address space

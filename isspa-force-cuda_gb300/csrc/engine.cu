@@ -497,6 +497,47 @@ struct isspa_engine {
         return (int)std::min<long long>(g, std::max(1, integrator_max_blocks()));
     }
 
+    // The single-kernel step needs split-4 field tiles (128-thread blocks), the
+    // LJ table in shared memory, Philox points and the tabulated LJ term on
+    // (or no IS-SPA pass); other engines step with separate kernels.
+    bool step_kernel_ok() const {
+        return n_atoms > 0 && !inject && n_lj_types * n_lj_types <= 4096 &&
+               (opt.isspa_terms == 0 || (opt.isspa_terms & 2)) && force_apt == 1;
+    }
+    StepArgs step_args() const {
+        StepArgs a{};
+        a.field = field_args();
+        a.field.vote = 0;
+        a.field.tma = 0;
+        a.force = force_args();
+        a.force.vote = 0;
+        a.nonbond = nonbond_args();
+        a.integ = integrator_args();
+        return a;
+    }
+    int step_grid() const {
+        const long long t = step_threads();
+        const long long terms = (long long)n_bonds + n_angles + n_dihs;
+        long long g = std::max<long long>({(long long)(opt.isspa_terms ? n_field_tiles : 0),
+                                           (long long)(opt.isspa_terms ? n_force_items : 0),
+                                           (long long)(opt.nonbond_terms ? n_nb_items : 0), (terms + t - 1) / t,
+                                           (n_atoms + t - 1) / t, (long long)n_us, 1LL});
+        return (int)std::min<long long>(g, std::max(1, step_max_blocks(n_lj_types)));
+    }
+    // Switches the step integrator; the single-kernel step takes split-4 field
+    // tiles (the split in force before it is restored when leaving it).
+    int split_before_step = 0;
+    void set_integrator(int m) {
+        if (m == 3 && !step_kernel_ok()) m = 1;
+        if (m == 3 && integrator != 3) {
+            split_before_step = field_split;
+            if (field_split != 4) set_field_split(4);
+        } else if (m != 3 && integrator == 3 && split_before_step && split_before_step != field_split) {
+            set_field_split(split_before_step);
+        }
+        integrator = m;
+    }
+
     // ---------------------------------------------------------- sequences
     void enqueue_isspa(cudaStream_t s, bool raw = false) {
         launch_field(field_args(), field_split, raw, s);
@@ -511,10 +552,12 @@ struct isspa_engine {
     }
     // Which kernels a step launches (the wrappers skip empty work lists).
     bool launches(int k) const {
+        const bool one = integrator == 3;
         switch (k) {
-            case ISSPA_K_FIELD: return opt.isspa_terms && n_field_tiles > 0;
-            case ISSPA_K_FORCE: return opt.isspa_terms && n_force_items > 0;
-            case ISSPA_K_NONBOND: return opt.nonbond_terms && n_nb_items > 0;
+            case ISSPA_K_FIELD: return !one && opt.isspa_terms && n_field_tiles > 0;
+            case ISSPA_K_FORCE: return !one && opt.isspa_terms && n_force_items > 0;
+            case ISSPA_K_NONBOND: return !one && opt.nonbond_terms && n_nb_items > 0;
+            case ISSPA_K_STEP: return one && n_atoms > 0;
             case ISSPA_K_BONDED: return integrator == 1 && n_bonds + n_angles + n_dihs > 0;
             case ISSPA_K_UMBRELLA: return integrator == 1 && n_us > 0;
             case ISSPA_K_LEAPFROG: return integrator == 1 && n_atoms > 0;
@@ -531,6 +574,12 @@ struct isspa_engine {
         auto mark = [&](int k, int end, cudaStream_t s) {
             if (timed && launches(k)) ck(cudaEventRecordWithFlags(kev[2 * k + end], s, cudaEventRecordExternal));
         };
+        if (integrator == 3) {  // the whole step in one cooperative kernel
+            mark(ISSPA_K_STEP, 0, stream);
+            if (n_atoms > 0) ck(launch_step(step_args(), step_grid(), stream));
+            mark(ISSPA_K_STEP, 1, stream);
+            return;
+        }
         ck(cudaEventRecord(ev_fork, stream));
         ck(cudaStreamWaitEvent(side, ev_fork, 0));
         mark(ISSPA_K_FIELD, 0, stream);
@@ -935,7 +984,8 @@ void build(isspa_engine &E, const std::vector<isspa_host_system> &ws) {
     E.usf = E.alloc<double2>(2 * (size_t)W);
     E.bar = E.alloc<unsigned int>(2);
     ck(cudaMemset(E.bar, 0, 2 * sizeof(unsigned int)));
-    E.integrator = E.opt.integrator == 2 ? 2 : 1;
+    E.integrator = 1;
+    if (E.opt.integrator == 2 || E.opt.integrator == 3) E.set_integrator(E.opt.integrator);
     E.integ_grid = E.integrator_grid();
     E.status = E.alloc<int>(1);
     E.d_step = E.alloc<uint32_t>(1);
@@ -1446,9 +1496,10 @@ int isspa_autotune(isspa_engine *e, int reps, int shape[ISSPA_SHAPE_COUNT]) {
             ck(cudaMemcpyAsync(v0.data(), e->vel, sizeof(float4) * e->n_atoms, cudaMemcpyDeviceToHost, e->stream));
             ck(cudaMemcpyAsync(&st0, e->d_step, sizeof(uint32_t), cudaMemcpyDeviceToHost, e->stream));
             ck(cudaStreamSynchronize(e->stream));
-            float t[3] = {0.f, 0.f, 0.f};
-            for (int m : {1, 2}) {
-                e->integrator = m;
+            float t[4] = {0.f, 0.f, 0.f, 1e30f};
+            for (int m : {1, 2, 3}) {
+                if (m == 3 && !e->step_kernel_ok()) continue;
+                e->set_integrator(m);
                 e->invalidate_graphs();
                 cudaGraphExec_t g = e->capture(1);
                 auto one = [&] { ck(cudaGraphLaunch(g, e->stream)); };
@@ -1459,7 +1510,10 @@ int isspa_autotune(isspa_engine *e, int reps, int shape[ISSPA_SHAPE_COUNT]) {
                 reps = saved;
                 cudaGraphExecDestroy(g);
             }
-            e->integrator = t[2] < t[1] ? 2 : 1;
+            int best_m = 1;
+            for (int m : {2, 3})
+                if (t[m] < t[best_m]) best_m = m;
+            e->set_integrator(best_m);
             ck(cudaMemcpyAsync(e->pos, p0.data(), sizeof(float4) * e->n_atoms, cudaMemcpyHostToDevice, e->stream));
             ck(cudaMemcpyAsync(e->vel, v0.data(), sizeof(float4) * e->n_atoms, cudaMemcpyHostToDevice, e->stream));
             ck(cudaMemcpyAsync(e->d_step, &st0, sizeof(uint32_t), cudaMemcpyHostToDevice, e->stream));

@@ -19,11 +19,13 @@
 //          FP32 partial sums are flushed once per stage into int64 fixed-point
 //          registers and once per item into the atom's accumulator, so the
 //          final force is independent of scheduling order.
+#include <algorithm>
 #include <cuda_runtime.h>
 
 #include <type_traits>
 
 #include "kernels.h"
+#include "md_device.cuh"
 #include "philox.h"
 
 namespace isspa {
@@ -100,11 +102,6 @@ __device__ __forceinline__ void bulk_load(void *dst, const void *src, unsigned b
 // Waits for phase `parity` of the barrier with non-blocking polls; false once
 // kBulkWaitNs of global time have passed (a deadline in time, not in polls).
 constexpr unsigned long long kBulkWaitNs = 1000000000ull;
-__device__ __forceinline__ unsigned long long global_ns() {
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
 __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity) {
     const unsigned long long t0 = global_ns();
     for (;;) {
@@ -136,7 +133,7 @@ struct FieldShape {
 // makes a bounded wait that gave up block-uniform: the block then flags
 // kStatusTimeout, waits (bounded) for its copies still in flight and exits.
 template <int S, bool GEN, bool RAW, bool VOTE, bool TMA = false>
-__global__ void __launch_bounds__(FieldShape<S>::kThreads) field_kernel(FieldArgs a) {
+__device__ __forceinline__ void field_tile(const FieldArgs &a, int tile_index) {
     constexpr int kT = FieldShape<S>::kThreads;
     // atoms staged per round: four per thread below a split of 4, so the
     // warps' compute phases between barriers are four times longer (64 windows
@@ -151,7 +148,7 @@ __global__ void __launch_bounds__(FieldShape<S>::kThreads) field_kernel(FieldArg
     constexpr bool kShareDraws = GEN && S >= 4;
     __shared__ float s_pt[3][kShareDraws ? kT / S : 1];  // the block's points, drawn once
 
-    const int4 tile = a.tiles[blockIdx.x];
+    const int4 tile = a.tiles[tile_index];
     const WinDev W = a.win[tile.x];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int grp = warp / S, sp = warp % S;
@@ -411,6 +408,11 @@ __global__ void __launch_bounds__(FieldShape<S>::kThreads) field_kernel(FieldArg
     a.out.q4[pg] = make_float4(fmaf(a1, hx, cd * fx), fmaf(a1, hy, cd * fy), fmaf(a1, hz, cd * fz), 1.5f * a3);
 }
 
+template <int S, bool GEN, bool RAW, bool VOTE, bool TMA = false>
+__global__ void __launch_bounds__(FieldShape<S>::kThreads) field_kernel(FieldArgs a) {
+    field_tile<S, GEN, RAW, VOTE, TMA>(a, blockIdx.x);
+}
+
 // One MC point's records side by side in shared memory: a single base address
 // per point, the five float4 at immediate offsets (q3 / q4 picked per lane).
 struct alignas(16) PointRec {
@@ -434,12 +436,11 @@ struct ForceShape {
 // branch.  Same operations in the same order as the per-pair loop.  It keeps
 // four points' geometry live (64 registers, 8 blocks per SM).
 template <bool LJ, int A, bool VOTE = false>
-__global__ void __launch_bounds__(ForceShape<A>::kThreads, VOTE ? 8 : ForceShape<A>::kMinBlocks)
-    force_kernel(ForceArgs a) {
+__device__ __forceinline__ void force_item(const ForceArgs &a, int item_index) {
     static_assert(!VOTE || A == 1, "the voted loop takes one receiving atom per thread");
     constexpr int kT = ForceShape<A>::kThreads;
     __shared__ PointRec s_p[kForceThreads];
-    const int4 item = a.items[blockIdx.x];
+    const int4 item = a.items[item_index];
     const WinDev W = a.win[item.x];
     const int2 ch = a.chunks[item.w];
     const int t = threadIdx.x;
@@ -477,11 +478,13 @@ __global__ void __launch_bounds__(ForceShape<A>::kThreads, VOTE ? 8 : ForceShape
         __syncthreads();
         for (int i = t; i < pn; i += kT) {
             const long long pg = (long long)ch.x + p0 + i;
-            s_p[i].q[0] = a.pts.q0[pg];
-            s_p[i].q[1] = a.pts.q1[pg];
-            s_p[i].q[2] = a.pts.q2[pg];
-            s_p[i].q[3] = a.pts.q3[pg];
-            s_p[i].q[4] = a.pts.q4[pg];
+            // through L2: in the single-kernel step the records were written
+            // by other blocks of the same launch
+            s_p[i].q[0] = __ldcg(a.pts.q0 + pg);
+            s_p[i].q[1] = __ldcg(a.pts.q1 + pg);
+            s_p[i].q[2] = __ldcg(a.pts.q2 + pg);
+            s_p[i].q[3] = __ldcg(a.pts.q3 + pg);
+            s_p[i].q[4] = __ldcg(a.pts.q4 + pg);
         }
         __syncthreads();
         // the pair (staged point k, receiving atom u) after its geometry; FAR:
@@ -577,6 +580,37 @@ __global__ void __launch_bounds__(ForceShape<A>::kThreads, VOTE ? 8 : ForceShape
     }
 }
 
+template <bool LJ, int A, bool VOTE = false>
+__global__ void __launch_bounds__(ForceShape<A>::kThreads, VOTE ? 8 : ForceShape<A>::kMinBlocks)
+    force_kernel(ForceArgs a) {
+    force_item<LJ, A, VOTE>(a, blockIdx.x);
+}
+
+// The whole MD step in one cooperative launch, for engines whose step is
+// latency-bound (a few thousand atoms or fewer): every kernel of a step would
+// otherwise pay its own launch, ramp-up and drain.  Phase 1: field tiles
+// (split 4), nonbond items, bonded terms and the restraint COMs (none of them
+// needs another's result); grid barrier; phase 2: force items; grid barrier;
+// phase 3: restraint forces and leapfrog per atom, step counter.  Each phase
+// runs the separate kernels' per-item code, so for the same work lists the
+// trajectory is bit-identical to theirs.  Both barriers are bounded (the
+// fused integrator's); a barrier that gives up flags kStatusTimeout and the
+// step integrates nothing.
+template <bool NB_ALL>
+__global__ void __launch_bounds__(kFieldThreads, 4) step_kernel(StepArgs a) {
+    extern __shared__ float2 s_ab[];
+    const uint32_t step = *a.integ.lf.step_ptr;
+    if (a.nonbond.n_items > 0) stage_ljab(a.nonbond, s_ab);
+    for (int t = blockIdx.x; t < a.field.n_tiles; t += gridDim.x) field_tile<4, true, false, false>(a.field, t);
+    for (int t = blockIdx.x; t < a.nonbond.n_items; t += gridDim.x) nonbond_item<true, NB_ALL>(a.nonbond, t, s_ab);
+    bonded_terms(a.integ.bonded);
+    restraint_coms(a.integ);
+    if (!grid_barrier(a.integ.bar, a.integ.lf.status)) return;
+    for (int t = blockIdx.x; t < a.force.n_items; t += gridDim.x) force_item<true, 1, false>(a.force, t);
+    if (!grid_barrier(a.integ.bar, a.integ.lf.status)) return;
+    integrate_atoms(a.integ, step);
+}
+
 template <int S, bool GEN, bool RAW, bool VOTE = false, bool TMA = false>
 void launch_field_t(const FieldArgs &a, cudaStream_t s) {
     field_kernel<S, GEN, RAW, VOTE, TMA><<<a.n_tiles, FieldShape<S>::kThreads, 0, s>>>(a);
@@ -641,6 +675,35 @@ int force_blocks_per_sm(int atoms_per_thread) {
     else
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, force_kernel<true, 1>, ForceShape<1>::kThreads, 0);
     return n;
+}
+
+int step_threads() { return kFieldThreads; }
+
+int step_max_blocks(int n_lj_types) {
+    int dev = 0, sms = 0, per_a = 0, per_b = 0;
+    const size_t smem = sizeof(float2) * (size_t)std::max(1, n_lj_types * n_lj_types);
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_a, step_kernel<true>, kFieldThreads, smem) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_b, step_kernel<false>, kFieldThreads, smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return sms * std::min(per_a, per_b);
+}
+
+cudaError_t launch_step(const StepArgs &a, int grid, cudaStream_t s) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(kFieldThreads);
+    cfg.dynamicSmemBytes = sizeof(float2) * (size_t)std::max(1, a.nonbond.n_lj_types * a.nonbond.n_lj_types);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (a.nonbond.terms == 7) return cudaLaunchKernelEx(&cfg, step_kernel<true>, a);
+    return cudaLaunchKernelEx(&cfg, step_kernel<false>, a);
 }
 
 void launch_force(const ForceArgs &a, cudaStream_t s) {

@@ -137,6 +137,14 @@ struct IntegratorArgs {
     unsigned int *bar;         // grid barrier: arrival count, generation (zero at rest)
 };
 
+// The whole MD step of an engine in one cooperative launch (see step_kernel).
+struct StepArgs {
+    FieldArgs field;
+    ForceArgs force;
+    NonbondArgs nonbond;
+    IntegratorArgs integ;
+};
+
 struct ListArgs {
     const float4 *pos;
     const int *excl_start;
@@ -219,6 +227,11 @@ void launch_leapfrog(const LeapfrogArgs &a, cudaStream_t s);
 cudaError_t launch_integrator(const IntegratorArgs &a, int grid, cudaStream_t s);
 int integrator_max_blocks();
 int integrator_block_threads();
+// Cooperative launch of the single-kernel step (field split 4, one receiving
+// atom per force thread, LJ table in shared memory, tabulated LJ term on).
+cudaError_t launch_step(const StepArgs &a, int grid, cudaStream_t s);
+int step_max_blocks(int n_lj_types);
+int step_threads();
 void launch_neighbor_list(const ListArgs &a, cudaStream_t s);
 // Up to three float4 arrays of n elements copied element-wise (a null source
 // skips its pair): state moved between the engine's device arrays and

@@ -138,7 +138,7 @@ class Engine:
         abi.check(abi.lib().isspa_time_steps(self._h, int(nsteps), int(flush_bytes), C.byref(ms)), "time")
         return ms.value
 
-    KERNELS = ("field", "force", "nonbond", "bonded", "umbrella", "leapfrog", "integrator")
+    KERNELS = ("field", "force", "nonbond", "bonded", "umbrella", "leapfrog", "integrator", "step")
 
     def time_steps_detailed(self, nsteps: int, flush_bytes: int = 0):
         """Device time of `nsteps` graph-replayed steps and of every kernel in them."""

@@ -12,6 +12,9 @@
   kernel) gives the separate kernels' trajectory bit for bit: a plain
   system, a restrained batch of windows, and the reference's ADI2 inputs
   with its umbrella restraint.
+* The single-kernel step (field, nonbond, bonded | force | update in one
+  cooperative kernel) gives the separate kernels' trajectory bit for bit with
+  the same launch shapes, on the same three systems.
 * The autotuner's integrator choice leaves the state where it was.
 * The grid barrier's bounded wait: a barrier left mid-count runs out,
   the step reports ISSPA_ERR_TIMEOUT without a fault, and the same engine
@@ -125,9 +128,9 @@ def test_near_minimum_stretch_and_bend_match_fp64_oracle():
         assert err <= 1e-5 * max(scale, 1e-3)
 
 
-def _trajectories(windows, steps, **opts):
+def _trajectories(windows, steps, modes=(1, 2), **opts):
     out = []
-    for integ in (1, 2):
+    for integ in modes:
         eng = ig.Engine(windows, integrator=integ, **opts)
         assert eng.shapes()["integrator"] == integ
         eng.step(steps)
@@ -136,8 +139,7 @@ def _trajectories(windows, steps, **opts):
     return out
 
 
-@pytest.mark.parametrize("which", ["medium", "batched-umbrella", "adi2-umbrella"])
-def test_fused_integrator_bit_identical(which, adi2):
+def _windows(which, adi2):
     if which == "medium":
         wins = ig.synth.make_system(12, 22, 34.0, 20, seed=21, ff=ig.synth.forcefield(n_mc=20))
         wins.pnu = 0.2
@@ -151,12 +153,30 @@ def test_fused_integrator_bit_identical(which, adi2):
         s.us_k, s.us_x0 = 20.0, 10.0
         s.pnu = 0.05
         wins = s
-    (p1, v1, _, c1, st1, ds1), (p2, v2, _, c2, st2, ds2) = _trajectories(wins, 12)
+    return wins
+
+
+@pytest.mark.parametrize("which", ["medium", "batched-umbrella", "adi2-umbrella"])
+def test_fused_integrator_bit_identical(which, adi2):
+    (p1, v1, _, c1, st1, ds1), (p2, v2, _, c2, st2, ds2) = _trajectories(_windows(which, adi2), 12)
     assert ds1 == 0 and ds2 == 0
     assert st1 == st2 == 12
     assert np.array_equal(p1, p2)
     assert np.array_equal(v1, v2)
     assert np.array_equal(c1[0], c2[0]) and np.array_equal(c1[1], c2[1])
+
+
+@pytest.mark.parametrize("which", ["medium", "batched-umbrella", "adi2-umbrella"])
+def test_single_kernel_step_bit_identical(which, adi2):
+    """The whole step as one cooperative kernel against the separate kernels,
+    both with split-4 field tiles and the same work lists."""
+    (p1, v1, _, c1, st1, ds1), (p3, v3, _, c3, st3, ds3) = _trajectories(_windows(which, adi2), 12, modes=(1, 3),
+                                                                         field_split=4)
+    assert ds1 == 0 and ds3 == 0
+    assert st1 == st3 == 12
+    assert np.array_equal(p1, p3)
+    assert np.array_equal(v1, v3)
+    assert np.array_equal(c1[0], c3[0]) and np.array_equal(c1[1], c3[1])
 
 
 def test_autotune_restores_state():
@@ -166,7 +186,7 @@ def test_autotune_restores_state():
     a.step(3)
     b.step(3)
     sh = a.autotune()
-    assert sh["integrator"] in (1, 2)
+    assert sh["integrator"] in (1, 2, 3)
     assert a.get_step() == 3
     assert np.array_equal(a.positions(), b.positions())
     assert np.array_equal(a.velocities(), b.velocities())
@@ -176,14 +196,16 @@ def test_autotune_restores_state():
     assert np.allclose(a.positions(), b.positions(), rtol=0, atol=1e-4)
 
 
-def test_fused_integrator_barrier_timeout_is_reported():
+@pytest.mark.parametrize("mode", [2, 3], ids=["fused-integrator", "single-kernel-step"])
+def test_grid_barrier_timeout_is_reported(mode):
     """A grid barrier left mid-count (as after a lost block) never completes:
     every block's bounded wait runs out, the step reports ISSPA_ERR_TIMEOUT,
     nothing faults, and after the status reset the engine steps on cleanly
     from a valid state."""
     s = ig.synth.config_small(seed=1)
-    eng = ig.Engine(s, integrator=2)
-    ref = ig.Engine(s, integrator=2)
+    eng = ig.Engine(s, integrator=mode)
+    ref = ig.Engine(s, integrator=mode)
+    assert eng.shapes()["integrator"] == mode
     L = abi.lib()
     abi.check(L.isspa_debug_stall_barrier(eng._h), "stall barrier")
     eng.step(1)
