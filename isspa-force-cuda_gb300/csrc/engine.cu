@@ -518,9 +518,9 @@ struct isspa_engine {
     int step_grid() const {
         const long long t = step_threads();
         const long long terms = (long long)n_bonds + n_angles + n_dihs;
-        long long g = std::max<long long>({(long long)(opt.isspa_terms ? n_field_tiles : 0),
-                                           (long long)(opt.isspa_terms ? n_force_items : 0),
-                                           (long long)(opt.nonbond_terms ? n_nb_items : 0), (terms + t - 1) / t,
+        long long g = std::max<long long>({(long long)(opt.isspa_terms ? n_field_tiles : 0) +
+                                               (long long)(opt.nonbond_terms ? n_nb_items : 0),
+                                           (long long)(opt.isspa_terms ? n_force_items : 0), (terms + t - 1) / t,
                                            (n_atoms + t - 1) / t, (long long)n_us, 1LL});
         return (int)std::min<long long>(g, std::max(1, step_max_blocks(n_lj_types)));
     }
@@ -1496,20 +1496,25 @@ int isspa_autotune(isspa_engine *e, int reps, int shape[ISSPA_SHAPE_COUNT]) {
             ck(cudaMemcpyAsync(v0.data(), e->vel, sizeof(float4) * e->n_atoms, cudaMemcpyDeviceToHost, e->stream));
             ck(cudaMemcpyAsync(&st0, e->d_step, sizeof(uint32_t), cudaMemcpyDeviceToHost, e->stream));
             ck(cudaStreamSynchronize(e->stream));
-            float t[4] = {0.f, 0.f, 0.f, 1e30f};
-            for (int m : {1, 2, 3}) {
-                if (m == 3 && !e->step_kernel_ok()) continue;
-                e->set_integrator(m);
-                e->invalidate_graphs();
-                cudaGraphExec_t g = e->capture(1);
-                auto one = [&] { ck(cudaGraphLaunch(g, e->stream)); };
-                const float first = time_it(one);
-                const int saved = reps;
-                reps = first > 2.0f ? saved : std::max(saved, 20);
-                t[m] = time_it(one);
-                reps = saved;
-                cudaGraphExecDestroy(g);
-            }
+            // three interleaved rounds, the minimum per mode: the modes differ
+            // by a few per cent where they differ at all
+            float t[4] = {0.f, 1e30f, 1e30f, 1e30f};
+            int rounds = 3;
+            for (int round = 0; round < rounds; ++round)
+                for (int m : {1, 2, 3}) {
+                    if (m == 3 && !e->step_kernel_ok()) continue;
+                    e->set_integrator(m);
+                    e->invalidate_graphs();
+                    cudaGraphExec_t g = e->capture(1);
+                    auto one = [&] { ck(cudaGraphLaunch(g, e->stream)); };
+                    const float first = time_it(one);
+                    if (first > 2.0f) rounds = 1;  // long steps: one round is enough
+                    const int saved = reps;
+                    reps = first > 2.0f ? saved : std::max(saved, 50);
+                    t[m] = std::min(t[m], time_it(one));
+                    reps = saved;
+                    cudaGraphExecDestroy(g);
+                }
             int best_m = 1;
             for (int m : {2, 3})
                 if (t[m] < t[best_m]) best_m = m;

@@ -601,8 +601,13 @@ __global__ void __launch_bounds__(kFieldThreads, 4) step_kernel(StepArgs a) {
     extern __shared__ float2 s_ab[];
     const uint32_t step = *a.integ.lf.step_ptr;
     if (a.nonbond.n_items > 0) stage_ljab(a.nonbond, s_ab);
-    for (int t = blockIdx.x; t < a.field.n_tiles; t += gridDim.x) field_tile<4, true, false, false>(a.field, t);
-    for (int t = blockIdx.x; t < a.nonbond.n_items; t += gridDim.x) nonbond_item<true, NB_ALL>(a.nonbond, t, s_ab);
+    // field tiles and nonbond items as one list over the blocks, so a block
+    // left without a tile takes a nonbond item instead of queueing behind one
+    const int n1 = a.field.n_tiles + a.nonbond.n_items;
+    for (int t = blockIdx.x; t < n1; t += gridDim.x) {
+        if (t < a.field.n_tiles) field_tile<4, true, false, false>(a.field, t);
+        else nonbond_item<true, NB_ALL>(a.nonbond, t - a.field.n_tiles, s_ab);
+    }
     bonded_terms(a.integ.bonded);
     restraint_coms(a.integ);
     if (!grid_barrier(a.integ.bar, a.integ.lf.status)) return;
