@@ -497,6 +497,18 @@ def run_precision(ig, args, peak_fp32):
     eng.zero_forces()
     status = eng.device_status()
     eng.close()
+    # the optional cutoff mode of the nonbond pass (12 A, skin 2 A) on the same
+    # configuration: the first call builds the neighbour list, later calls find
+    # no atom moved and run the displacement check and the pairs only
+    ec = ig.Engine(s, nonbond_cutoff=12.0)
+    ec.zero_forces()
+    first = ec.nonbond_force(True)
+    steady = min(ec.nonbond_force(True) for _ in range(5))
+    cut = {"cutoff_A": 12.0, "skin_A": 2.0, "ms_first_call_with_build": round(first, 4),
+           "ms_per_call_without_build": round(steady, 4), "list": ec.nonbond_list_stats(),
+           "rows": ec.shapes()["nonbond_list_rows"], "cells": ec.shapes()["nonbond_list_cells"],
+           "device_status": ec.device_status()}
+    ec.close()
     avg = {k: v[0] / v[1] for k, v in kern.items() if v[1] > 0}
     force_tf = FLOP_FORCE_PAIR * N * P / (avg["force"] * 1e-3) / 1e12
     field_tf = (FLOP_FIELD_PAIR * N * P + FLOP_POINT * P) / (avg["field"] * 1e-3) / 1e12
@@ -508,6 +520,7 @@ def run_precision(ig, args, peak_fp32):
             "kernel_ms_alone": alone,
             "nonbond_alone_tflops": round(FLOP_NB_PAIR * N * (N - 1) / (alone["nonbond"] * 1e-3) / 1e12, 2),
             "nonbond_alone_frac": round(FLOP_NB_PAIR * N * (N - 1) / (alone["nonbond"] * 1e-3) / 1e12 / peak_fp32, 4),
+            "nonbond_cutoff_mode": cut,
             "force_kernel_tflops": round(force_tf, 2), "force_kernel_frac": round(force_tf / peak_fp32, 4),
             "field_kernel_tflops": round(field_tf, 2), "field_kernel_frac": round(field_tf / peak_fp32, 4),
             "launch_shapes": shapes, "device_status": status,
@@ -580,6 +593,66 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def run_variants(args):
+    """A/B of the engine's result-preserving variants on each workload, with
+    every other launch shape at the autotuner's choice: the three step modes
+    (1 two-branch graph of separate kernels, 2 fused cooperative integrator,
+    3 single-kernel cooperative step, the last with split-4 field tiles and
+    per-pair loops as it runs them) and the field pass's atom staging (thread
+    loads against 1-D bulk copies).  Step times are single-step graph
+    replays (CUDA events, 256 MB written between steps); back-to-back runs of
+    8-step graphs by the host clock; kernel times from the event-instrumented
+    step."""
+    import build as engine_build
+    import isspa_gb300 as ig
+
+    engine_build.build()
+
+    def adi2():
+        w = ig.System.from_config(os.path.join(ROOT, "tests", "golden", "adi2_config.txt"))
+        w.n_mc = 100
+        w.pnu = 0.02
+        return w
+
+    cases = [("44 atoms, nMC 20", lambda: ig.synth.config_small(seed=1), 400),
+             ("ADI2 44 atoms, nMC 100, 200 A box", adi2, 400),
+             ("1100 atoms, nMC 50", lambda: ig.synth.config_plain(seed=2), 400),
+             ("64 windows, 41 206 atoms", lambda: ig.synth.config_batched(n_windows=64, seed=4), 60)]
+    out = {}
+    for name, make, steps in cases:
+        system = make()
+        e = ig.Engine(system)
+        tuned = e.autotune()
+        e.close()
+        base = {k: int(tuned[k]) for k in ("field_split", "force_chunk", "force_tail_chunk",
+                                            "force_atoms_per_thread", "field_vote", "force_vote")}
+        base["nonbond_chunk"] = int(tuned["nonbond_partners_per_item"])
+        res = {"autotuned": tuned}
+        runs = [(f"mode{m}", m, 0) for m in (1, 2, 3)] + [("mode1_field_tma", 1, 1)]
+        for label, mode, tma in runs:
+            o = dict(base, integrator=mode, field_tma=tma)
+            if mode == 3:
+                o.update(field_split=4, field_vote=0, force_vote=0)
+            e = ig.Engine(system, **o)
+            e.step(20)
+            ms = e.time_steps(steps, L2_FLUSH) / steps
+            n = 4000 if ms < 0.1 else 200
+            e.synchronize()
+            t0 = time.perf_counter()
+            e.step(n)
+            e.synchronize()
+            run_ms = (time.perf_counter() - t0) / n * 1e3
+            _, kern = e.time_steps_detailed(min(steps, 50), L2_FLUSH)
+            res[label] = {"integrator": e.shapes()["integrator"], "field_tma": e.shapes()["field_tma"],
+                          "step_ms": round(ms, 5), "run_ms_per_step": round(run_ms, 5),
+                          "kernel_ms": {k: round(v[0] / v[1], 5) for k, v in kern.items() if v[1]},
+                          "device_status": e.device_status()}
+            e.close()
+        out[name] = res
+    print(json.dumps({"variants": out, "timing": "step_ms: single-step graph replays, CUDA events, 256 MB "
+                      "written between steps; run_ms_per_step: back-to-back 8-step graphs, host clock"}))
+
+
 def _cu_profiler(on: bool):
     """cuProfilerStart/Stop of the driver API: with `ncu --profile-from-start
     off` only the launches in between are profiled."""
@@ -601,12 +674,33 @@ def run_profile_case(args):
 
     engine_build.build()
     if args.workload == "batched":
-        eng = ig.Engine(ig.synth.config_batched(n_windows=64, seed=4))
+        system = ig.synth.config_batched(n_windows=64, seed=4)
     elif args.workload == "precision":
-        eng = ig.Engine(ig.synth.config_precision(seed=3))
+        system = ig.synth.config_precision(seed=3)
     else:
-        eng = ig.Engine(ig.synth.config_plain(seed=2))
-    shapes = eng.shapes() if args.no_autotune else eng.autotune()
+        system = ig.synth.config_plain(seed=2)
+    fixed = None
+    if args.shapes_file and os.path.exists(args.shapes_file):
+        with open(args.shapes_file) as f:
+            fixed = json.load(f)
+    if fixed is not None:
+        # the shapes an earlier run of this command chose: an ncu run replays them
+        # instead of autotuning under the profiler, whose serialised launches
+        # would favour other shapes
+        eng = ig.Engine(system, field_split=fixed["field_split"], force_chunk=fixed["force_chunk"],
+                        force_atoms_per_thread=fixed["force_atoms_per_thread"],
+                        force_tail_chunk=fixed["force_tail_chunk"], field_vote=fixed["field_vote"],
+                        force_vote=fixed["force_vote"], integrator=fixed["integrator"],
+                        nonbond_chunk=fixed["nonbond_partners_per_item"], field_tma=fixed["field_tma"])
+        shapes = eng.shapes()
+        if shapes != fixed:
+            raise RuntimeError(f"shapes from {args.shapes_file} not reproduced: {shapes} != {fixed}")
+    else:
+        eng = ig.Engine(system)
+        shapes = eng.shapes() if args.no_autotune else eng.autotune()
+        if args.shapes_file:
+            with open(args.shapes_file, "w") as f:
+                json.dump(shapes, f)
     eng.step(2)
     eng.synchronize()
     _cu_profiler(True)
@@ -622,6 +716,8 @@ def main():
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="run this many untimed graph steps and exit (profiling case)")
     ap.add_argument("--workload", default="plain", choices=["plain", "batched", "precision"])
+    ap.add_argument("--shapes-file", default="",
+                    help="profiling case: launch shapes to use; written by the autotuner when absent")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=5)
@@ -631,6 +727,8 @@ def main():
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the precision-workload and adjoint sections")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--variants", action="store_true",
+                    help="A/B the step modes and the field pass's staging on four workloads and exit")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank = int(os.environ.get("RANK", "0"))
@@ -638,6 +736,8 @@ def main():
         return  # replicas only: the engine runs on one GPU; other ranks do no work
     if args.profile_steps > 0:
         run_profile_case(args)
+    elif args.variants:
+        run_variants(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -42,6 +42,7 @@ extern "C" {
 #define ISSPA_ERR_UNSUPPORTED (-9)  /* input outside what the engine supports */
 #define ISSPA_ERR_STATE (-10)       /* call not valid in the engine's state */
 #define ISSPA_ERR_OVERFLOW (-11)    /* a force exceeded the fixed-point range */
+#define ISSPA_ERR_LIST_FULL (-12)   /* a neighbour-list row outgrew its capacity (cutoff mode) */
 
 /* ---- system description (plain arrays) ---------------------------------- */
 /* One simulation window: everything the reference's atom / bond / angle / dih
@@ -134,6 +135,23 @@ typedef struct isspa_engine_options {
     int field_tma;       /* 1: the field pass stages each round of 128 atoms with a 1-D bulk
                             copy (cp.async.bulk, the TMA engine) behind an mbarrier, double-
                             buffered (same results); 0 => coalesced loads by the threads */
+    float nonbond_cutoff;  /* > 0: cutoff mode of the nonbond pass -- only pairs whose FP32
+                              squared minimum-image distance is below cutoff^2 (A) count, with
+                              LJ, Coulomb and the IS-SPA correction all truncated there (no
+                              shift; energies likewise), found through a Verlet neighbour list
+                              over per-window cell lists that the device rebuilds whenever an
+                              atom has moved more than half the skin since the last build.
+                              The forces do not depend on the skin or on when the list was
+                              rebuilt.  Not available to isspa_adjoint_mean_force
+                              (ISSPA_ERR_UNSUPPORTED) or to the single-kernel step (integrator 3
+                              falls back to 1).  0 => every pair (the reference's behaviour: its
+                              config `cutoff` reaches the nonbond kernel unused); < 0 or
+                              non-finite => ISSPA_ERR_ARG */
+    float nonbond_skin;    /* Verlet buffer of the neighbour list (A); 0 => 2 */
+    int nonbond_list_max;  /* partners a neighbour-list row holds; 0 => 1.5 x the fullest row
+                              of the starting configuration + 32 (at most the largest window).
+                              A row that outgrows it reports ISSPA_ERR_LIST_FULL through
+                              isspa_device_status (the forces of that step are incomplete) */
 } isspa_engine_options;
 
 #define ISSPA_TERMS_NONE (-1)
@@ -198,8 +216,10 @@ int isspa_engine_info(const isspa_engine *e, int *n_windows, int *n_atoms_total,
  * none), [9] 1 when the field pass walks its atoms in warp-voted groups,
  * [10] 1 when the force pass takes its points in warp-voted groups, [11] the
  * step integrator (1 separate kernels, 2 fused, 3 single-kernel step; see isspa_engine_options),
- * [12] 1 when the field pass stages its atoms by bulk copies (TMA). */
-#define ISSPA_SHAPE_COUNT 13
+ * [12] 1 when the field pass stages its atoms by bulk copies (TMA), [13] in
+ * cutoff mode the partners a neighbour-list row holds (0 otherwise), [14] in
+ * cutoff mode the cells of all windows' cell grids (0 otherwise). */
+#define ISSPA_SHAPE_COUNT 15
 int isspa_engine_shapes(const isspa_engine *e, int shape[ISSPA_SHAPE_COUNT]);
 /* Autotuner: times every field-pass atom split (per-pair and warp-voted
  * loops, atoms staged by loads or by bulk copies) and, for 1 and 2 receiving
@@ -255,6 +275,12 @@ void isspa_host_free(void *p);
 int isspa_synchronize(isspa_engine *e);
 /* Sticky device status word (0 if nothing tripped); clears it when reset != 0. */
 int isspa_device_status(isspa_engine *e, int reset);
+/* Cutoff mode (no counterpart on the reference's live path; its dead
+ * neighborlist_cuda.cu:11-137 / cell_list_cuda.cu:13-35 are the closest):
+ * how many times the neighbour list has been built since the engine was made,
+ * and the fullest row of the last build (partners within cutoff + skin).
+ * Synchronises the engine stream.  ISSPA_ERR_STATE without a cutoff. */
+int isspa_nonbond_list_stats(isspa_engine *e, int *builds, int *fullest_row);
 /* Failure-detection testing (no counterpart in the reference): leaves the
  * fused integrator's grid barrier as if a block had been lost mid-count, so the
  * next fused step's bounded waits run out; that step integrates nothing and

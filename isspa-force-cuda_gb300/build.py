@@ -25,7 +25,8 @@ LIB = os.path.join(HERE, "libisspa_gb300.so")
 EXE = os.path.join(HERE, "total_force_gb300")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["engine.cu", "k_isspa.cu", "k_md.cu", "k_adjoint.cu", "k_energy.cu", "k_noalloc.cu", "io.cpp"]
+SOURCES = ["engine.cu", "k_isspa.cu", "k_md.cu", "k_nblist.cu", "k_adjoint.cu", "k_energy.cu", "k_noalloc.cu",
+           "io.cpp"]
 
 
 def nvcc() -> str:

@@ -26,6 +26,7 @@ enum : int {
     kStatusNonFinite = 2,
     kStatusBounds = 4,
     kStatusTimeout = 8,  // a bounded device wait gave up
+    kStatusListFull = 16,  // a neighbour-list row outgrew its capacity
 };
 
 // One window (umbrella window or replica) of a batch.

@@ -103,6 +103,15 @@ struct isspa_engine {
     int4 *nb_items = nullptr;
     int *nb_nj = nullptr;
     int n_nb_items = 0, nb_chunk = 0, n_sms = 0;
+    // cutoff mode of the nonbond pass (nonbond_cutoff > 0): Verlet list over cell lists
+    bool cutoff = false;
+    float nb_cut2 = 0.f, nb_list2 = 0.f, nb_half_skin2 = 0.f;
+    int4 *nbl_wcell = nullptr;
+    float4 *nbl_ref = nullptr;
+    int *nbl_flag = nullptr, *nbl_stats = nullptr;
+    int *nbl_cell_of = nullptr, *nbl_cell_count = nullptr, *nbl_cell_start = nullptr, *nbl_cell_cursor = nullptr,
+        *nbl_cell_atoms = nullptr, *nbl_rows = nullptr, *nbl_row_n = nullptr;
+    int nbl_cells = 0, nbl_row_cap = 0;
     int4 *bonds = nullptr, *angles = nullptr, *dihs = nullptr;
     float2 *bond_par = nullptr, *angle_par = nullptr, *sc14 = nullptr;
     float4 *angle_cs = nullptr;
@@ -403,9 +412,55 @@ struct isspa_engine {
         a.excl_start = excl_start;
         a.excl = excl;
         a.terms = opt.nonbond_terms;
+        a.cut2 = cutoff ? nb_cut2 : INFINITY;
         a.facc = facc;
         a.status = status;
         return a;
+    }
+    NbListArgs nblist_args() const {
+        NbListArgs a{};
+        a.pos = pos;
+        a.atype = atype;
+        a.atom_win = atom_win;
+        a.win = win;
+        a.wcell = nbl_wcell;
+        a.n_atoms = n_atoms;
+        a.n_cells = nbl_cells;
+        a.ref = nbl_ref;
+        a.flag = nbl_flag;
+        a.stats = nbl_stats;
+        a.cell_of = nbl_cell_of;
+        a.cell_count = nbl_cell_count;
+        a.cell_start = nbl_cell_start;
+        a.cell_cursor = nbl_cell_cursor;
+        a.cell_atoms = nbl_cell_atoms;
+        a.rows = nbl_rows;
+        a.row_n = nbl_row_n;
+        a.row_cap = nbl_row_cap;
+        a.half_skin2 = nb_half_skin2;
+        a.list2 = nb_list2;
+        a.cut2 = nb_cut2;
+        a.excl_start = excl_start;
+        a.excl = excl;
+        a.ljab = ljab;
+        a.n_lj_types = n_lj_types;
+        a.rmax = rmax;
+        a.terms = opt.nonbond_terms;
+        a.facc = facc;
+        a.status = status;
+        return a;
+    }
+    // The nonbond pass: every pair, or in cutoff mode the list check / rebuild
+    // and the pairs within the cutoff.
+    void enqueue_nonbond(cudaStream_t s) const {
+        if (!opt.nonbond_terms) return;
+        if (cutoff) {
+            const NbListArgs a = nblist_args();
+            launch_nblist_build(a, s);
+            launch_nblist_pairs(a, s);
+        } else {
+            launch_nonbond(nonbond_args(), s);
+        }
     }
     BondedArgs bonded_args(int b, int an, int d) const {
         BondedArgs a{};
@@ -501,7 +556,7 @@ struct isspa_engine {
     // LJ table in shared memory, Philox points and the tabulated LJ term on
     // (or no IS-SPA pass); other engines step with separate kernels.
     bool step_kernel_ok() const {
-        return n_atoms > 0 && !inject && n_lj_types * n_lj_types <= 4096 &&
+        return n_atoms > 0 && !inject && !cutoff && n_lj_types * n_lj_types <= 4096 &&
                (opt.isspa_terms == 0 || (opt.isspa_terms & 2)) && force_apt == 1;
     }
     StepArgs step_args() const {
@@ -546,7 +601,7 @@ struct isspa_engine {
     void enqueue_step_serial(cudaStream_t s) {
         launch_bonded(bonded_args(1, 1, 1), s);
         enqueue_isspa(s);
-        launch_nonbond(nonbond_args(), s);
+        enqueue_nonbond(s);
         launch_umbrella(umbrella_args(), s);
         launch_leapfrog(leapfrog_args(), s);
     }
@@ -556,7 +611,7 @@ struct isspa_engine {
         switch (k) {
             case ISSPA_K_FIELD: return !one && opt.isspa_terms && n_field_tiles > 0;
             case ISSPA_K_FORCE: return !one && opt.isspa_terms && n_force_items > 0;
-            case ISSPA_K_NONBOND: return !one && opt.nonbond_terms && n_nb_items > 0;
+            case ISSPA_K_NONBOND: return !one && opt.nonbond_terms && (cutoff ? n_atoms > 0 : n_nb_items > 0);
             case ISSPA_K_STEP: return one && n_atoms > 0;
             case ISSPA_K_BONDED: return integrator == 1 && n_bonds + n_angles + n_dihs > 0;
             case ISSPA_K_UMBRELLA: return integrator == 1 && n_us > 0;
@@ -597,7 +652,7 @@ struct isspa_engine {
             mark(ISSPA_K_UMBRELLA, 1, side);
         }
         mark(ISSPA_K_NONBOND, 0, side);
-        launch_nonbond(nonbond_args(), side);
+        enqueue_nonbond(side);
         mark(ISSPA_K_NONBOND, 1, side);
         ck(cudaEventRecord(ev_join, side));
         ck(cudaStreamWaitEvent(stream, ev_join, 0));
@@ -753,6 +808,8 @@ void expand_lj(int nlj, const std::vector<int> &nbp, const std::vector<float> &l
     ljab.resize((size_t)nlj * nlj);
     for (int i = 0; i < nlj * nlj; ++i) ljab[i] = make_float2(lj_ab[2 * nbp[i]], lj_ab[2 * nbp[i] + 1]);
 }
+
+void build_nonbond_list(isspa_engine &E);
 
 void build(isspa_engine &E, const std::vector<isspa_host_system> &ws) {
     const isspa_host_system &f0 = ws[0];
@@ -985,6 +1042,7 @@ void build(isspa_engine &E, const std::vector<isspa_host_system> &ws) {
     E.bar = E.alloc<unsigned int>(2);
     ck(cudaMemset(E.bar, 0, 2 * sizeof(unsigned int)));
     E.integrator = 1;
+    E.cutoff = E.opt.nonbond_cutoff > 0.f;  // (its list is built below) no single-kernel step
     if (E.opt.integrator == 2 || E.opt.integrator == 3) E.set_integrator(E.opt.integrator);
     E.integ_grid = E.integrator_grid();
     E.status = E.alloc<int>(1);
@@ -993,6 +1051,75 @@ void build(isspa_engine &E, const std::vector<isspa_host_system> &ws) {
     ck(cudaMemset(E.status, 0, sizeof(int)));
     ck(cudaMemset(E.d_step, 0, sizeof(uint32_t)));
     ck(cudaMemset(E.d_done, 0, sizeof(unsigned int)));
+    if (E.opt.nonbond_cutoff > 0.f) build_nonbond_list(E);
+}
+
+// Cutoff mode of the nonbond pass: per-window cell grids (cells at least
+// 1.0001 (cutoff + skin) on a side, at most about 8 per atom, the whole window
+// as one cell below 3 per edge), the list buffers, and the row capacity -- the
+// option, or 1.5 x the fullest row of the starting configuration + 32 (at most
+// the largest window), found by a counting pass of the list build.
+void build_nonbond_list(isspa_engine &E) {
+    const float rc = E.opt.nonbond_cutoff;
+    const float skin = E.opt.nonbond_skin > 0.f ? E.opt.nonbond_skin : 2.0f;
+    const float rl = rc + skin;
+    E.cutoff = true;
+    E.nb_cut2 = rc * rc;
+    E.nb_list2 = rl * rl;
+    // rebuild beyond 0.499 skin (not 0.5): a margin far above the rounding of
+    // the FP32 displacement and distance checks
+    const float half = 0.499f * skin;
+    E.nb_half_skin2 = half * half;
+    const int W = E.n_windows;
+    std::vector<int4> wcell(W);
+    long long cells = 0;
+    int max_n = 1;
+    for (int w = 0; w < W; ++w) {
+        const WinDev &d = E.win_h[w];
+        max_n = std::max(max_n, d.n_atoms);
+        const double geo = std::floor((double)d.box / (1.0001 * (double)rl));
+        const double cap = std::floor(std::cbrt(8.0 * std::max(d.n_atoms, 1)));
+        const int nc = std::min(geo, cap) >= 3.0 ? (int)std::min(geo, cap) : 1;
+        const float scale = (float)nc / d.box;
+        int bits = 0;
+        std::memcpy(&bits, &scale, sizeof bits);
+        wcell[w] = make_int4((int)cells, nc, bits, 0);
+        cells += (long long)nc * nc * nc;
+    }
+    if (cells > INT32_MAX / 2) throw Fail{ISSPA_ERR_UNSUPPORTED};
+    E.nbl_cells = (int)cells;
+    const size_t N = (size_t)E.n_atoms;
+    E.nbl_wcell = E.upload(wcell);
+    E.nbl_ref = E.alloc<float4>(N);
+    E.nbl_flag = E.alloc<int>(1);
+    E.nbl_stats = E.alloc<int>(2);
+    E.nbl_cell_of = E.alloc<int>(N);
+    E.nbl_cell_count = E.alloc<int>(cells);
+    E.nbl_cell_start = E.alloc<int>(cells + 1);
+    E.nbl_cell_cursor = E.alloc<int>(cells);
+    E.nbl_cell_atoms = E.alloc<int>(N);
+    E.nbl_row_n = E.alloc<int>(N);
+    ck(cudaMemset(E.nbl_cell_count, 0, sizeof(int) * cells));
+    auto reset = [&] {  // NaN reference positions: the next check rebuilds
+        ck(cudaMemset(E.nbl_ref, 0xff, sizeof(float4) * N));
+        ck(cudaMemset(E.nbl_flag, 0, sizeof(int)));
+        ck(cudaMemset(E.nbl_stats, 0, 2 * sizeof(int)));
+    };
+    reset();
+    int cap = E.opt.nonbond_list_max;
+    if (cap <= 0) {
+        NbListArgs a = E.nblist_args();
+        a.rows = nullptr;
+        launch_nblist_build(a, E.stream);
+        ck(cudaGetLastError());
+        int st[2] = {0, 0};
+        ck(cudaMemcpyAsync(st, E.nbl_stats, sizeof st, cudaMemcpyDeviceToHost, E.stream));
+        ck(cudaStreamSynchronize(E.stream));
+        cap = ((st[1] * 3 / 2 + 32 + 31) / 32) * 32;
+        reset();
+    }
+    E.nbl_row_cap = std::max(1, std::min(cap, max_n));
+    E.nbl_rows = E.alloc<int>(N * (size_t)E.nbl_row_cap);
 }
 
 int guard(isspa_engine *e) {
@@ -1048,6 +1175,7 @@ const char *isspa_strerror(int s) {
         case ISSPA_ERR_UNSUPPORTED: return "input outside what the engine supports";
         case ISSPA_ERR_STATE: return "call not valid in the engine state";
         case ISSPA_ERR_OVERFLOW: return "force outside the fixed-point range";
+        case ISSPA_ERR_LIST_FULL: return "a neighbour-list row outgrew its capacity";
         default: return "unknown status";
     }
 }
@@ -1094,6 +1222,9 @@ int isspa_engine_create(const isspa_system_desc *windows, int n_windows, const i
     else if (e->opt.isspa_terms == 0) e->opt.isspa_terms = 7;
     if (e->opt.nonbond_terms < 0) e->opt.nonbond_terms = 0;
     else if (e->opt.nonbond_terms == 0) e->opt.nonbond_terms = 7;
+    if (!(e->opt.nonbond_cutoff >= 0.f) || !(e->opt.nonbond_skin >= 0.f) || e->opt.nonbond_list_max < 0 ||
+        std::isinf(e->opt.nonbond_cutoff) || std::isinf(e->opt.nonbond_skin))
+        return ISSPA_ERR_ARG;
     if (cudaGetDevice(&e->device) != cudaSuccess) {
         cudaGetLastError();
         return ISSPA_ERR_CUDA;
@@ -1147,6 +1278,8 @@ int isspa_engine_shapes(const isspa_engine *e, int shape[ISSPA_SHAPE_COUNT]) {
     shape[10] = e->force_apt == 1 ? e->force_vote : 0;
     shape[11] = e->integrator;
     shape[12] = e->field_tma;
+    shape[13] = e->cutoff ? e->nbl_row_cap : 0;
+    shape[14] = e->cutoff ? e->nbl_cells : 0;
     return ISSPA_OK;
 }
 
@@ -1186,6 +1319,8 @@ int isspa_adjoint_mean_force(isspa_engine *e, int n_frames, const float *frames,
     if (rc) return rc;
     // the gradient kernels differentiate the full force (every term)
     if ((e->opt.isspa_terms & 7) != 7 || (e->opt.nonbond_terms & 7) != 7) return ISSPA_ERR_STATE;
+    // its pair kernels differentiate every pair, not the truncated force
+    if (e->cutoff) return ISSPA_ERR_UNSUPPORTED;
     const int W = e->n_windows, N = e->n_atoms;
     const long long P = e->n_points;
     const long long nF = (long long)e->n_itypes * e->n_f, nG = (long long)e->n_itypes * e->n_g;
@@ -1365,7 +1500,7 @@ int isspa_energies(isspa_engine *e, double *out) {
         // the forces of the current step, in the reference order
         launch_bonded(e->bonded_args(1, 1, 1), s);
         e->enqueue_isspa(s);
-        launch_nonbond(e->nonbond_args(), s);
+        e->enqueue_nonbond(s);
         launch_umbrella(e->umbrella_args(), s);
         // energies of the same configuration, and the kick the forces give
         launch_nonbond_energy(e->nonbond_args(), e->energy, s);
@@ -1468,7 +1603,7 @@ int isspa_autotune(isspa_engine *e, int reps, int shape[ISSPA_SHAPE_COUNT]) {
             e->force_vote = voted < plain ? 1 : 0;
         }
         // nonbond pass: partner stretches per item (results do not move)
-        if (e->opt.nonbond_terms && e->n_nb_items > 0) {
+        if (e->opt.nonbond_terms && e->n_nb_items > 0 && !e->cutoff) {
             int maxN = 0;
             for (const WinDev &d : e->win_h) maxN = std::max(maxN, d.n_atoms);
             float bestn = 1e30f;
@@ -1550,7 +1685,7 @@ int isspa_force_cuda(isspa_engine *e, float *ms) {
     return timed_call(e, ms, [&] { e->enqueue_isspa(e->stream); });
 }
 int nonbond_force_cuda(isspa_engine *e, float *ms) {
-    return timed_call(e, ms, [&] { launch_nonbond(e->nonbond_args(), e->stream); });
+    return timed_call(e, ms, [&] { e->enqueue_nonbond(e->stream); });
 }
 int us_force_cuda(isspa_engine *e, float *ms) {
     return timed_call(e, ms, [&] { launch_umbrella(e->umbrella_args(), e->stream); });
@@ -1706,6 +1841,24 @@ int isspa_device_status(isspa_engine *e, int reset) {
     if (st & kStatusNonFinite) return ISSPA_ERR_NONFINITE;
     if (st & kStatusOverflow) return ISSPA_ERR_OVERFLOW;
     if (st & kStatusBounds) return ISSPA_ERR_BOUNDS;
+    if (st & kStatusListFull) return ISSPA_ERR_LIST_FULL;
+    return ISSPA_OK;
+}
+
+int isspa_nonbond_list_stats(isspa_engine *e, int *builds, int *fullest_row) {
+    if (!e || !builds || !fullest_row) return ISSPA_ERR_ARG;
+    int rc = guard(e);
+    if (rc) return rc;
+    if (!e->cutoff) return ISSPA_ERR_STATE;
+    int st[2] = {0, 0};
+    rc = run_guarded([&] {
+        ck(cudaStreamSynchronize(e->stream));
+        ck(cudaMemcpyAsync(st, e->nbl_stats, sizeof st, cudaMemcpyDeviceToHost, e->stream));
+        ck(cudaStreamSynchronize(e->stream));
+    });
+    if (rc) return rc;
+    *builds = st[0];
+    *fullest_row = st[1];
     return ISSPA_OK;
 }
 

@@ -116,6 +116,7 @@ __global__ void __launch_bounds__(kEnThreads) nonbond_energy_kernel(NonbondArgs 
             const float ry = mimg(xi.y - xj.y, L, h);
             const float rz = mimg(xi.z - xj.z, L, h);
             const float d2 = dist2f(rx, ry, rz);
+            if (d2 >= a.cut2) continue;  // cutoff mode: the truncated potential
             const float ri = rsqrtf(d2);
             const float qq = xi.w * xj.w;
             if (terms & 4) {

@@ -68,6 +68,35 @@ struct NonbondArgs {
     const int *excl_start;     // [Ntot+1] CSR of symmetric exclusions (global, sorted)
     const int *excl;
     int terms;                 // 1 LJ, 2 Coulomb, 4 IS-SPA correction
+    float cut2;                // pair energies: squared cutoff (+inf: every pair)
+    unsigned long long *facc;
+    int *status;
+};
+
+// ---- cutoff nonbond: Verlet neighbour list over cell lists ---------------
+struct NbListArgs {
+    const float4 *pos;
+    const int2 *atype;
+    const int *atom_win;
+    const WinDev *win;
+    const int4 *wcell;         // per window: first cell, cells per edge (1: one cell), bits of nc / box, -
+    int n_atoms;               // all windows
+    int n_cells;               // all windows
+    float4 *ref;               // [Ntot] positions at the last build (NaN before the first)
+    int *flag;                 // 1: rebuild this step
+    int *stats;                // builds so far, fullest row of the last build
+    int *cell_of, *cell_count, *cell_start, *cell_cursor, *cell_atoms;
+    int *rows;                 // [Ntot][row_cap] partner | excluded << 31 (nullptr: counts only)
+    int *row_n;                // [Ntot] partners found (may exceed row_cap)
+    int row_cap;
+    float half_skin2;          // (skin / 2)^2
+    float list2;               // (cutoff + skin)^2
+    float cut2;                // cutoff^2
+    const int *excl_start, *excl;
+    const float2 *ljab;
+    int n_lj_types;
+    const float *rmax;
+    int terms;                 // 1 LJ, 2 Coulomb, 4 IS-SPA correction
     unsigned long long *facc;
     int *status;
 };
@@ -219,6 +248,9 @@ void launch_adjoint(const AdjointArgs &a, cudaStream_t s);
 void launch_field(const FieldArgs &a, int split, bool raw, cudaStream_t s);
 void launch_force(const ForceArgs &a, cudaStream_t s);
 void launch_nonbond(const NonbondArgs &a, cudaStream_t s);
+// Cutoff mode: displacement check and (when it trips) the list rebuild; then the pairs.
+void launch_nblist_build(const NbListArgs &a, cudaStream_t s);
+void launch_nblist_pairs(const NbListArgs &a, cudaStream_t s);
 void launch_bonded(const BondedArgs &a, cudaStream_t s);
 void launch_umbrella(const UmbrellaArgs &a, cudaStream_t s);
 void launch_leapfrog(const LeapfrogArgs &a, cudaStream_t s);

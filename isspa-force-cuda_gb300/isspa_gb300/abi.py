@@ -14,6 +14,7 @@ LIB_PATH = os.path.join(PKG_DIR, "libisspa_gb300.so")
 OK = 0
 ERR_ARG, ERR_IO, ERR_PARSE, ERR_CUDA, ERR_NOMEM = -1, -2, -3, -4, -5
 ERR_BOUNDS, ERR_TIMEOUT, ERR_NONFINITE, ERR_UNSUPPORTED, ERR_STATE, ERR_OVERFLOW = -6, -7, -8, -9, -10, -11
+ERR_LIST_FULL = -12
 
 
 class IsspaError(RuntimeError):
@@ -52,7 +53,8 @@ class EngineOptions(C.Structure):
                 ("field_split", C.c_int), ("force_chunk", C.c_int), ("mem_cap", C.c_size_t),
                 ("force_atoms_per_thread", C.c_int), ("force_tail_chunk", C.c_int),
                 ("field_vote", C.c_int), ("force_vote", C.c_int), ("integrator", C.c_int),
-                ("nonbond_chunk", C.c_int), ("field_tma", C.c_int)]
+                ("nonbond_chunk", C.c_int), ("field_tma", C.c_int), ("nonbond_cutoff", C.c_float),
+                ("nonbond_skin", C.c_float), ("nonbond_list_max", C.c_int)]
 
 
 class RunConfig(C.Structure):
@@ -79,7 +81,7 @@ class NoallocInputs(C.Structure):
 NOALLOC_SCRATCH_BYTES = 16 << 20
 # ISSPA_NOALLOC_STATUS_* bits written to isspa_noalloc_inputs.status_out
 NOALLOC_STATUS_OVERFLOW, NOALLOC_STATUS_NONFINITE, NOALLOC_STATUS_BOUNDS = 1, 2, 4
-SHAPE_COUNT = 13  # ISSPA_SHAPE_COUNT
+SHAPE_COUNT = 15  # ISSPA_SHAPE_COUNT
 TERMS_NONE = -1  # ISSPA_TERMS_NONE: switches the IS-SPA or nonbond pass off
 
 # isspa_energies components (the ISSPA_E_* enum), kcal/mol
@@ -124,6 +126,7 @@ SIGNATURES = [
     ("isspa_host_free", None, [_P]),
     ("isspa_synchronize", C.c_int, [_P]),
     ("isspa_device_status", C.c_int, [_P, C.c_int]),
+    ("isspa_nonbond_list_stats", C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     ("isspa_debug_stall_barrier", C.c_int, [_P]),
     ("isspa_set_positions", C.c_int, [_P, _P, C.c_int]),
     ("isspa_get_positions", C.c_int, [_P, _P, C.c_int]),

@@ -25,7 +25,8 @@ class Engine:
                  nonbond_terms: int = 7, use_graph: bool = True, field_split: int = 0,
                  force_chunk: int = 0, mem_cap: int = 0, force_atoms_per_thread: int = 0,
                  force_tail_chunk: int = 0, field_vote: int = 0, force_vote: int = 0, integrator: int = 0,
-                 nonbond_chunk: int = 0, field_tma: int = 0):
+                 nonbond_chunk: int = 0, field_tma: int = 0, nonbond_cutoff: float = 0.0,
+                 nonbond_skin: float = 0.0, nonbond_list_max: int = 0):
         if isinstance(windows, System):
             windows = [windows]
         self.windows = list(windows)
@@ -48,6 +49,9 @@ class Engine:
         opt.integrator = int(integrator)
         opt.nonbond_chunk = int(nonbond_chunk)
         opt.field_tma = int(field_tma)
+        opt.nonbond_cutoff = float(nonbond_cutoff)
+        opt.nonbond_skin = float(nonbond_skin)
+        opt.nonbond_list_max = int(nonbond_list_max)
         h = C.c_void_p()
         abi.check(L.isspa_engine_create(descs, len(self.windows), C.byref(opt), C.byref(h)), "engine create")
         self._h = h
@@ -61,8 +65,14 @@ class Engine:
         abi.check(abi.lib().isspa_engine_shapes(self._h, v), "shapes")
         keys = ("field_split", "field_tiles", "force_chunk", "force_items", "nonbond_items",
                 "nonbond_partners_per_item", "sms", "force_atoms_per_thread", "force_tail_chunk",
-                "field_vote", "force_vote", "integrator", "field_tma")
+                "field_vote", "force_vote", "integrator", "field_tma", "nonbond_list_rows", "nonbond_list_cells")
         return dict(zip(keys, list(v)))
+
+    def nonbond_list_stats(self) -> dict:
+        """Cutoff mode: list builds so far and the fullest row of the last build."""
+        b, m = C.c_int(), C.c_int()
+        abi.check(abi.lib().isspa_nonbond_list_stats(self._h, C.byref(b), C.byref(m)), "list stats")
+        return {"builds": b.value, "fullest_row": m.value}
 
     def autotune(self, reps: int = 3) -> dict:
         """Time candidate launch shapes on this workload and keep the fastest."""

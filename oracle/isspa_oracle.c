@@ -368,7 +368,10 @@ static int orc_excluded(const orc_nb_sys *s, int i, int j) {
  * r^-6(12A r^-6 - 6B)/r^2 (:131-132) + Coulomb q1q2/r^3 (:136) + correction;
  * excluded pairs: correction only (:153-162).  Correction (:141-147): r >
  * 2 rmax[type j] => -2q1q2(1-1/ep)/(3r^3), else -q1q2(1-1/ep)(8rmax-3r)/(24
- * rmax^4).  Force on atom i only.
+ * rmax^4).  Force on atom i only.  With s->cut2 > 0 (the engine's optional
+ * cutoff mode, not on the reference's live path) a pair counts only when its
+ * FP32 squared minimum-image distance is below cut2: all three terms
+ * truncated there, no shift.
  * ------------------------------------------------------------------------- */
 static void nonbond_impl(const orc_nb_sys *s, int term_mask, const int *atoms, int n_sel, double *f);
 
@@ -395,6 +398,7 @@ static void nonbond_impl(const orc_nb_sys *s, int term_mask, const int *atoms, i
             const float ry = mimg(xi[1] - xj[1], L, h);
             const float rz = mimg(xi[2] - xj[2], L, h);
             const float d2 = dist2f(rx, ry, rz);
+            if (s->cut2 > 0.0f && !(d2 < s->cut2)) continue;
             const double dx = rx, dy = ry, dz = rz;
             const double dd2 = dx * dx + dy * dy + dz * dz;
             const double dd = sqrt(dd2);
@@ -855,6 +859,7 @@ void orc_energies(const orc_nb_sys *s, int nb_terms, int n_bonds, const int *bon
             const float ry = mimg(xi[1] - xj[1], L, h);
             const float rz = mimg(xi[2] - xj[2], L, h);
             const float d2 = dist2f(rx, ry, rz);
+            if (s->cut2 > 0.0f && !(d2 < s->cut2)) continue;
             const double dd2 = (double)rx * rx + (double)ry * ry + (double)rz * rz, dd = sqrt(dd2);
             const double qq = (double)xi[3] * (double)xj[3];
             const float rmj = s->rmax[s->isspa_type[j]];

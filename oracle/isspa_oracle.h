@@ -58,6 +58,8 @@ typedef struct {
     const int *isspa_type;     /* [n_atoms] */
     const float *rmax;         /* [n_itypes] */
     float box;
+    float cut2;                /* > 0: only pairs with FP32 squared distance below it count
+                                  (the engine's optional cutoff mode); 0: every pair */
 } orc_nb_sys;
 
 /* Term masks, naming follows the reference's per-term golden files. */

@@ -44,7 +44,7 @@ class _NbSys(C.Structure):
     _fields_ = [("n_atoms", C.c_int), ("pos", C.c_void_p), ("n_types", C.c_int),
                 ("lj_type", C.c_void_p), ("nb_parm_index", C.c_void_p), ("lj_ab", C.c_void_p),
                 ("n_excl_cum", C.c_void_p), ("excl_list", C.c_void_p),
-                ("isspa_type", C.c_void_p), ("rmax", C.c_void_p), ("box", C.c_float)]
+                ("isspa_type", C.c_void_p), ("rmax", C.c_void_p), ("box", C.c_float), ("cut2", C.c_float)]
 
 
 _lib = None
@@ -83,9 +83,11 @@ class Oracle:
 
     Table values (ISSPA_DENSITIES / _EFIELD / _FORCES, LJ A and B) are held in
     FP64; `tables` may supply FP64 values that override the system's float ones
-    (finite differences in the force-field parameters)."""
+    (finite differences in the force-field parameters).  `nonbond_cutoff` > 0
+    truncates the nonbond pairs and their energies at that distance (the
+    engine's optional cutoff mode; every pair counts otherwise)."""
 
-    def __init__(self, system, threads: int = 0, tables=None):
+    def __init__(self, system, threads: int = 0, tables=None, nonbond_cutoff: float = 0.0):
         s = system
         self.s = s
         self.n = int(s.n_atoms)
@@ -111,8 +113,9 @@ class Oracle:
         self.lj = lj
         exc = _i32(s.n_excl_cum); exl = _i32(s.excl_list if len(s.excl_list) else [-1])
         k.extend([ljt, nbp, lj, exc, exl])
+        rc = np.float32(nonbond_cutoff)
         self.nsys = _NbSys(self.n, _p(pos), int(s.n_lj_types), _p(ljt), _p(nbp), _p(lj),
-                           _p(exc), _p(exl), _p(ityp), _p(rmax), s.box)
+                           _p(exc), _p(exl), _p(ityp), _p(rmax), s.box, float(rc * rc) if rc > 0 else 0.0)
         L = lib()
         L.orc_set_threads(int(threads))
 
