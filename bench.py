@@ -677,6 +677,8 @@ def run_profile_case(args):
         system = ig.synth.config_batched(n_windows=64, seed=4)
     elif args.workload == "precision":
         system = ig.synth.config_precision(seed=3)
+    elif args.workload == "small":
+        system = ig.synth.config_small(seed=1)
     else:
         system = ig.synth.config_plain(seed=2)
     fixed = None
@@ -715,7 +717,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="run this many untimed graph steps and exit (profiling case)")
-    ap.add_argument("--workload", default="plain", choices=["plain", "batched", "precision"])
+    ap.add_argument("--workload", default="plain", choices=["plain", "batched", "precision", "small"])
     ap.add_argument("--shapes-file", default="",
                     help="profiling case: launch shapes to use; written by the autotuner when absent")
     ap.add_argument("--gpus", type=int, default=1)

@@ -64,8 +64,8 @@ inline void ck(cudaError_t e) {
 
 struct isspa_engine {
     int device = 0;
-    cudaStream_t stream = nullptr, side = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_a = nullptr, ev_b = nullptr;
+    cudaStream_t stream = nullptr, side = nullptr, side2 = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_join2 = nullptr, ev_a = nullptr, ev_b = nullptr;
     isspa_engine_options opt{};
     int n_windows = 0, n_atoms = 0, n_mc = 0;
     long long n_points = 0;
@@ -335,10 +335,11 @@ struct isspa_engine {
         for (auto ev : tev) cudaEventDestroy(ev);
         for (auto ev : kev)
             if (ev) cudaEventDestroy(ev);
-        for (cudaEvent_t ev : {ev_fork, ev_join, ev_a, ev_b})
+        for (cudaEvent_t ev : {ev_fork, ev_join, ev_join2, ev_a, ev_b})
             if (ev) cudaEventDestroy(ev);
         for (void *p : allocs) cudaFree(p);
         if (side) cudaStreamDestroy(side);
+        if (side2) cudaStreamDestroy(side2);
         if (stream) cudaStreamDestroy(stream);
     }
 
@@ -637,6 +638,7 @@ struct isspa_engine {
         }
         ck(cudaEventRecord(ev_fork, stream));
         ck(cudaStreamWaitEvent(side, ev_fork, 0));
+        ck(cudaStreamWaitEvent(side2, ev_fork, 0));
         mark(ISSPA_K_FIELD, 0, stream);
         launch_field(field_args(), field_split, false, stream);
         mark(ISSPA_K_FIELD, 1, stream);
@@ -651,11 +653,16 @@ struct isspa_engine {
             launch_umbrella(umbrella_args(), side);
             mark(ISSPA_K_UMBRELLA, 1, side);
         }
-        mark(ISSPA_K_NONBOND, 0, side);
-        enqueue_nonbond(side);
-        mark(ISSPA_K_NONBOND, 1, side);
+        // nonbond on a third branch: for small systems bonded + restraint and
+        // nonbond are each as long as the IS-SPA pass, and in series they
+        // were the step's critical path
+        mark(ISSPA_K_NONBOND, 0, side2);
+        enqueue_nonbond(side2);
+        mark(ISSPA_K_NONBOND, 1, side2);
         ck(cudaEventRecord(ev_join, side));
+        ck(cudaEventRecord(ev_join2, side2));
         ck(cudaStreamWaitEvent(stream, ev_join, 0));
+        ck(cudaStreamWaitEvent(stream, ev_join2, 0));
         if (integrator == 2) {
             mark(ISSPA_K_INTEGRATOR, 0, stream);
             if (n_atoms > 0) ck(launch_integrator(integrator_args(), integ_grid, stream));
@@ -1237,7 +1244,8 @@ int isspa_engine_create(const isspa_system_desc *windows, int n_windows, const i
         int prio_low = 0, prio_high = 0;
         ck(cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high));
         ck(cudaStreamCreateWithPriority(&e->side, cudaStreamNonBlocking, prio_high));
-        for (cudaEvent_t *ev : {&e->ev_fork, &e->ev_join})
+        ck(cudaStreamCreateWithPriority(&e->side2, cudaStreamNonBlocking, prio_high));
+        for (cudaEvent_t *ev : {&e->ev_fork, &e->ev_join, &e->ev_join2})
             ck(cudaEventCreateWithFlags(ev, cudaEventDisableTiming));
         ck(cudaEventCreate(&e->ev_a));
         ck(cudaEventCreate(&e->ev_b));
