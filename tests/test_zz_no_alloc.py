@@ -15,8 +15,9 @@ The tests drive it through the C ABI with device arrays the test allocates
   * that repeated calls leave the device's free memory unchanged;
   * a system just under the buffer's limit against the engine, and the
     first size beyond it rejected before anything is enqueued;
-  * the status word: a non-finite coordinate and an IS-SPA type outside the
-    table are reported through status_out (made on the host, no GPU fault),
+  * the status word: a non-finite coordinate, an IS-SPA type outside the
+    table and a charge large enough to push the forces beyond the fixed-point
+    range are reported through status_out (made on the host, no GPU fault),
     and the next clean call reports 0;
   * argument checks (terms outside 0..7).
 It lives in its own file that pytest collects last.
@@ -197,6 +198,16 @@ def test_noalloc_status_word(torch_dev, medium):
     assert rc == abi.OK
     assert status == abi.NOALLOC_STATUS_BOUNDS
     assert np.all(np.isfinite(got))
+    # a charge of 1e15 (the IS-SPA pass has no pair singularity to collapse:
+    # MC points never coincide with atoms): forces far beyond the fixed-point
+    # range are reported as overflow (or non-finite), and the call still
+    # returns ISSPA_OK with the status word set
+    u = medium.copy()
+    u.pos = u.pos.copy()
+    u.pos[5, 3] = 1.0e15
+    rc, got, status = Call(torch_dev, u).run(0)
+    assert rc == abi.OK
+    assert status & (abi.NOALLOC_STATUS_OVERFLOW | abi.NOALLOC_STATUS_NONFINITE)
     rc, got, status = Call(torch_dev, medium).run(0)
     assert rc == abi.OK and status == 0
 
