@@ -596,7 +596,7 @@ def run_reference(args):
 def run_variants(args):
     """A/B of the engine's result-preserving variants on each workload, with
     every other launch shape at the autotuner's choice: the three step modes
-    (1 two-branch graph of separate kernels, 2 fused cooperative integrator,
+    (1 branched graph of separate kernels, 2 fused cooperative integrator,
     3 single-kernel cooperative step, the last with split-4 field tiles and
     per-pair loops as it runs them) and the field pass's atom staging (thread
     loads against 1-D bulk copies).  Step times are single-step graph

@@ -1238,9 +1238,9 @@ int isspa_engine_create(const isspa_system_desc *windows, int n_windows, const i
     }
     int rc = run_guarded([&] {
         ck(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
-        // the second branch (bonded, umbrella, nonbond: a few hundred blocks)
-        // at the highest priority, so its blocks are dispatched ahead of the
-        // field and force grids' queued blocks instead of after them
+        // the side branches (bonded and umbrella; nonbond: a few hundred
+        // blocks) at the highest priority, so their blocks are dispatched ahead
+        // of the field and force grids' queued blocks instead of after them
         int prio_low = 0, prio_high = 0;
         ck(cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high));
         ck(cudaStreamCreateWithPriority(&e->side, cudaStreamNonBlocking, prio_high));
