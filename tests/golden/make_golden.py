@@ -49,6 +49,9 @@ def main(ref):
     shutil.copy(os.path.join(us, "ADI2.us"), os.path.join(HERE, "ADI2.us"))
     # step-0 total forces of the 10000MC run (nMC=1000, seed 8622; curand stream)
     shutil.copy(os.path.join(adi, "10000MC", "ADI.2.forces.xyz"), os.path.join(HERE, "ADI.2.forces.xyz"))
+    # the same run's IS-SPA output file: the tabulated-LJ term alone (the last
+    # frame of the LJsolv study, ISSPA_force_LJsolv_10000.xyz), same MC sample
+    shutil.copy(os.path.join(adi, "10000MC", "ISSPA_force.xyz"), os.path.join(HERE, "ADI2.ISSPA_force.step0.xyz"))
 
 
 if __name__ == "__main__":

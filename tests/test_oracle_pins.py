@@ -6,6 +6,9 @@
 * IS-SPA force branches against the reference's 1000-seed per-term frame
   averages at nMC = 1000 (ISSPA_force_{Csolv,LJsolv,Csolv_CDD}_10000.xyz),
   as a z-test of the means.
+* The reference's step-0 total force of one run (timing_tests/ADI2/10000MC/
+  ADI.2.forces.xyz: bonded + IS-SPA + nonbond, total_force_cuda.cpp:109-121)
+  against the oracle's bonded and nonbond terms plus its IS-SPA distribution.
 """
 import math
 import os
@@ -120,3 +123,41 @@ def test_oracle_determinism_and_step_keying(adi2):
     assert not np.array_equal(a, o.mc_points(seed=7, step=4))
     assert not np.array_equal(a, o.mc_points(seed=8, step=3))
     assert not np.array_equal(a, o.mc_points(seed=7, step=3, window=1))
+
+
+def _xyz_rows(path, n=44):
+    with open(path) as f:
+        lines = f.read().split("\n")[2:2 + n]
+    return np.array([[float(v) for v in line.split()[1:]] for line in lines])
+
+
+def test_step0_total_force_against_reference_output(adi2):
+    """One run of the reference (nMC 1000, 200 A box, its curand point stream)
+    wrote the step-0 total force (bonded, IS-SPA and nonbond) and, in its
+    IS-SPA output file, the tabulated mean-LJ term of the same MC sample
+    (that build's study of the LJsolv branch).  The total minus the oracle's
+    bonded and nonbond forces minus that recorded term is the run's multipole
+    + CDD sample: compared per component with the oracle's mean and spread
+    over 40 Philox samples at the same nMC (z-scores; the spread is ~0.3 % of
+    the total force, so a 1 % error in the bonded terms gives rms z ~ 25).
+    The recorded tabulated-LJ term is checked the same way."""
+    tot = _xyz_rows(os.path.join(GOLDEN, "ADI.2.forces.xyz"))
+    rec = _xyz_rows(os.path.join(GOLDEN, "ADI2.ISSPA_force.step0.xyz"))
+    assert np.allclose(rec[:, :3], adi2.pos[:, :3], atol=1e-5)
+    assert adi2.n_mc == 1000 and adi2.box == 200.0
+    o = O.Oracle(adi2)
+    det = o.bonded() + o.nonbond(O.NB_LJ | O.NB_COUL | O.NB_CORR)
+    mp, lj = [], []
+    for k in range(40):
+        pts = o.mc_points(seed=9000 + k, step=0)
+        fld = o.field(pts)
+        mp.append(o.isspa_force(pts, fld, O.MULTIPOLE | O.CDD))
+        lj.append(o.isspa_force(pts, fld, O.LJ_TAB))
+    for label, sample, dist in [("multipole + CDD", tot - det - rec[:, 3:], np.array(mp)),
+                                ("tabulated LJ", rec[:, 3:], np.array(lj))]:
+        sd = dist.std(0, ddof=1) * np.sqrt(1.0 + 1.0 / len(dist))
+        z = (sample - dist.mean(0)) / sd
+        rms, mx = float(np.sqrt(np.mean(z ** 2))), float(np.abs(z).max())
+        print(f"{label}: rms z {rms:.2f}, max |z| {mx:.2f} over {z.size} components")
+        assert rms < 1.5, label
+        assert mx < 4.5, label
