@@ -1586,11 +1586,12 @@ int isspa_autotune(isspa_engine *e, int reps, int shape[ISSPA_SHAPE_COUNT]) {
             // two waves of short ones
             std::vector<std::pair<int, int>> pairs;
             for (int c : cands) pairs.push_back({c, 0});
-            // (4- and 8-point tails: a system of a few dozen atoms has fewer points
-            // than one wave of 16-point items, and its step waits on the longest
-            // thread's chain of points)
+            // (8-point tails: a system of a few dozen atoms has fewer points than
+            // one wave of 16-point items, and its step waits on the longest
+            // thread's chain of points; 4-point tails timed faster alone but
+            // slower inside the step)
             for (int c : {64, 128, 256, 512, 1024})
-                for (int t : {4, 8, 16, 32, 64})
+                for (int t : {8, 16, 32, 64})
                     if (t < c && c <= std::max<long long>(128, maxP)) pairs.push_back({c, t});
             for (const auto &ct : pairs) {
                 e->set_force_chunk(ct.first, ct.second);
