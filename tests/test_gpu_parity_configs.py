@@ -8,7 +8,10 @@
     own FP64 fields at all 1.64 M points, then the IS-SPA, nonbond and bonded
     forces on 64 sampled atoms are compared with the engine's total force;
   * 64 umbrella windows of 44-1100 atoms in one engine with autotuned shapes:
-    the smallest, the largest and two other windows against the oracle.
+    the smallest, the largest and two other windows against the oracle;
+  * the 1100-atom system over 20 steps against the FP64-state oracle stepped
+    from the same state with the same Philox streams (positions and
+    velocities, 1e-4).
 Measures and tolerances: tests/parity.py (normwise and per atom, 1e-5).
 """
 import numpy as np
@@ -117,3 +120,36 @@ def test_batched_64_windows_autotuned():
         ref, _, c = O.Oracle(s).total_force(seed=s.seed, step=0, window=w)
         check_force(f[offs[w]:offs[w + 1]], ref, f"64-window batch, window {w} ({s.n_atoms} atoms)")
         assert np.allclose(com[w], c, atol=1e-9)
+
+
+def test_plain_1100_trajectory_tracks_fp64_oracle():
+    """The benchmarked 1100-atom system with the autotuned shapes stepped 20
+    times on the GPU and by the FP64-state oracle from the same state with the
+    same Philox streams (MC points and Andersen draws): positions and
+    velocities agree step by step up to the rounding of the state (each step's
+    force error against FP64 is ~5e-7 normwise), so every kernel of the step
+    and the update are pinned over a trajectory, not only at step 0."""
+    s = ig.synth.config_plain(seed=2)
+    eng = ig.Engine(s)
+    eng.autotune()
+    n = 20
+    eng.step(n)
+    assert eng.device_status() == 0
+    t = s.copy()
+    t.pos = np.ascontiguousarray(s.pos, np.float32).copy()
+    t.vel = np.ascontiguousarray(s.vel, np.float32).copy()
+    o = O.Oracle(t)  # reads o.pos / t.vel in place every call
+    for k in range(n):
+        f, _, _ = o.total_force(s.seed, k, 0)
+        po, vo, _ = o.leapfrog(f, s.seed, k, 0)
+        o.pos[:, :3] = po
+        t.vel[:, :3] = vo
+    L = float(s.box)
+    dx = eng.positions()[:, :3].astype(np.float64) - o.pos[:, :3]
+    dx -= L * np.round(dx / L)
+    dv = eng.velocities()[:, :3].astype(np.float64) - t.vel[:, :3]
+    vscale = float(np.abs(t.vel[:, :3]).max())
+    print(f"1100 atoms, {n} steps: max |dx| {np.abs(dx).max():.2e} A, max |dv| {np.abs(dv).max():.2e} "
+          f"(max |v| {vscale:.3e})")
+    assert np.abs(dx).max() < 1e-4
+    assert np.abs(dv).max() < 1e-4 * vscale
