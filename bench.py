@@ -598,8 +598,9 @@ def run_variants(args):
     every other launch shape at the autotuner's choice: the three step modes
     (1 branched graph of separate kernels, 2 fused cooperative integrator,
     3 single-kernel cooperative step, the last with split-4 field tiles and
-    per-pair loops as it runs them) and the field pass's atom staging (thread
-    loads against 1-D bulk copies).  Step times are single-step graph
+    per-pair loops as it runs them), modes 1 and 2 with the kernel chain
+    launched as programmatic dependents, and the field pass's atom staging
+    (thread loads against 1-D bulk copies).  Step times are single-step graph
     replays (CUDA events, 256 MB written between steps); back-to-back runs of
     8-step graphs by the host clock; kernel times from the event-instrumented
     step."""
@@ -628,9 +629,13 @@ def run_variants(args):
                                             "force_atoms_per_thread", "field_vote", "force_vote")}
         base["nonbond_chunk"] = int(tuned["nonbond_partners_per_item"])
         res = {"autotuned": tuned}
-        runs = [(f"mode{m}", m, 0) for m in (1, 2, 3)] + [("mode1_field_tma", 1, 1)]
-        for label, mode, tma in runs:
-            o = dict(base, integrator=mode, field_tma=tma)
+        # step_pdl 2: ordinary launches; 1: the field -> force -> leapfrog
+        # chain as programmatic dependents (the pair timed twice, interleaved)
+        runs = [("mode1", 1, 0, 2), ("mode1_pdl", 1, 0, 1), ("mode2", 2, 0, 2), ("mode2_pdl", 2, 0, 1),
+                ("mode3", 3, 0, 2), ("mode1_field_tma", 1, 1, 2), ("mode1_again", 1, 0, 2),
+                ("mode1_pdl_again", 1, 0, 1)]
+        for label, mode, tma, pdl in runs:
+            o = dict(base, integrator=mode, field_tma=tma, step_pdl=pdl)
             if mode == 3:
                 o.update(field_split=4, field_vote=0, force_vote=0)
             e = ig.Engine(system, **o)
@@ -644,6 +649,7 @@ def run_variants(args):
             run_ms = (time.perf_counter() - t0) / n * 1e3
             _, kern = e.time_steps_detailed(min(steps, 50), L2_FLUSH)
             res[label] = {"integrator": e.shapes()["integrator"], "field_tma": e.shapes()["field_tma"],
+                          "step_pdl": e.shapes()["step_pdl"],
                           "step_ms": round(ms, 5), "run_ms_per_step": round(run_ms, 5),
                           "kernel_ms": {k: round(v[0] / v[1], 5) for k, v in kern.items() if v[1]},
                           "device_status": e.device_status()}

@@ -152,6 +152,12 @@ typedef struct isspa_engine_options {
                               of the starting configuration + 32 (at most the largest window).
                               A row that outgrows it reports ISSPA_ERR_LIST_FULL through
                               isspa_device_status (the forces of that step are incomplete) */
+    int step_pdl;          /* 1: isspa_step launches the field, force and leapfrog kernels as
+                              programmatic dependents of the kernel before each on the stream
+                              (each waits for that kernel's completion before its first memory
+                              access, so its launch overlaps the other's tail; same results);
+                              2: ordinary launches; 0 => 2 until isspa_autotune times both and
+                              keeps the faster.  The single-kernel step has no chain */
 } isspa_engine_options;
 
 #define ISSPA_TERMS_NONE (-1)
@@ -218,8 +224,9 @@ int isspa_engine_info(const isspa_engine *e, int *n_windows, int *n_atoms_total,
  * step integrator (1 separate kernels, 2 fused, 3 single-kernel step; see isspa_engine_options),
  * [12] 1 when the field pass stages its atoms by bulk copies (TMA), [13] in
  * cutoff mode the partners a neighbour-list row holds (0 otherwise), [14] in
- * cutoff mode the cells of all windows' cell grids (0 otherwise). */
-#define ISSPA_SHAPE_COUNT 15
+ * cutoff mode the cells of all windows' cell grids (0 otherwise), [15] 1 when
+ * isspa_step launches its kernel chain as programmatic dependents. */
+#define ISSPA_SHAPE_COUNT 16
 int isspa_engine_shapes(const isspa_engine *e, int shape[ISSPA_SHAPE_COUNT]);
 /* Autotuner: times every field-pass atom split (per-pair and warp-voted
  * loops, atoms staged by loads or by bulk copies) and, for 1 and 2 receiving
@@ -229,9 +236,10 @@ int isspa_engine_shapes(const isspa_engine *e, int shape[ISSPA_SHAPE_COUNT]);
  * chosen list) on this engine's own
  * workload with CUDA events (reps launches each), keeps the fastest of each
  * and reports the result as isspa_engine_shapes does.  When the options leave
- * the integrator open (0), it then times single-step graph replays with the
- * separate and the fused integrator and keeps the faster (the nonbond
- * partners per item are timed too); positions,
+ * the integrator or step_pdl open (0), it then times single-step graph
+ * replays of the open choices (separate kernels, fused integrator,
+ * single-kernel step; with and without programmatic launches) and keeps the
+ * fastest (the nonbond partners per item are timed too); positions,
  * velocities and the step counter are restored.  Clears the force
  * accumulator; invalidates captured graphs. */
 int isspa_autotune(isspa_engine *e, int reps, int shape[ISSPA_SHAPE_COUNT]);

@@ -29,6 +29,15 @@ enum : int {
     kStatusListFull = 16,  // a neighbour-list row outgrew its capacity
 };
 
+// Programmatic dependent launch.  A kernel launched as a programmatic
+// dependent of the kernel before it on the stream may be scheduled while that
+// kernel still runs; pdl_wait() returns once every kernel it depends on has
+// completed and its memory is visible (at once for an ordinary launch), so it
+// comes before the kernel's first global access.  pdl_trigger() lets the next
+// kernel's blocks be scheduled once every block of this one has passed it.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // One window (umbrella window or replica) of a batch.
 struct WinDev {
     int atom_off, n_atoms;     // global atom range

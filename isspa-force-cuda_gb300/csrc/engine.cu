@@ -91,6 +91,7 @@ struct isspa_engine {
     int force_tail = 0;  // chunk length of the short items listed last (0: none)
     int field_vote = 0;  // field pass in warp-voted groups of four atoms
     int field_tma = 0;   // field pass stages its atom rounds by 1-D bulk copies (TMA)
+    int step_pdl = 0;    // step chain launched as programmatic dependents (1) or not (0)
     int force_vote = 0;  // force pass in warp-voted groups of four points (1 atom per thread)
     int force_apt = 1;  // receiving atoms per force-kernel thread (1 or 2)
     // step integrator: 1 = bonded, umbrella and leapfrog kernels (bonded and
@@ -630,6 +631,9 @@ struct isspa_engine {
         auto mark = [&](int k, int end, cudaStream_t s) {
             if (timed && launches(k)) ck(cudaEventRecordWithFlags(kev[2 * k + end], s, cudaEventRecordExternal));
         };
+        // programmatic launches for the field -> force -> leapfrog chain (not
+        // in the event-instrumented copy, whose event nodes sit between them)
+        PdlScope pdl(step_pdl == 1 && !timed && integrator != 3);
         if (integrator == 3) {  // the whole step in one cooperative kernel
             mark(ISSPA_K_STEP, 0, stream);
             if (n_atoms > 0) ck(launch_step(step_args(), step_grid(), stream));
@@ -969,6 +973,7 @@ void build(isspa_engine &E, const std::vector<isspa_host_system> &ws) {
     E.set_field_split(S);
     E.field_vote = E.opt.field_vote == 1 ? 1 : 0;
     E.field_tma = E.opt.field_tma == 1 ? 1 : 0;
+    E.step_pdl = E.opt.step_pdl == 1 ? 1 : 0;
     E.force_vote = E.opt.force_vote == 1 ? 1 : 0;
     E.force_apt = E.opt.force_atoms_per_thread == 2 ? 2 : 1;
     E.set_force_chunk(E.opt.force_chunk > 0 ? E.opt.force_chunk : E.default_force_chunk(),
@@ -1230,7 +1235,8 @@ int isspa_engine_create(const isspa_system_desc *windows, int n_windows, const i
     if (e->opt.nonbond_terms < 0) e->opt.nonbond_terms = 0;
     else if (e->opt.nonbond_terms == 0) e->opt.nonbond_terms = 7;
     if (!(e->opt.nonbond_cutoff >= 0.f) || !(e->opt.nonbond_skin >= 0.f) || e->opt.nonbond_list_max < 0 ||
-        std::isinf(e->opt.nonbond_cutoff) || std::isinf(e->opt.nonbond_skin))
+        std::isinf(e->opt.nonbond_cutoff) || std::isinf(e->opt.nonbond_skin) || e->opt.step_pdl < 0 ||
+        e->opt.step_pdl > 2)
         return ISSPA_ERR_ARG;
     if (cudaGetDevice(&e->device) != cudaSuccess) {
         cudaGetLastError();
@@ -1288,6 +1294,7 @@ int isspa_engine_shapes(const isspa_engine *e, int shape[ISSPA_SHAPE_COUNT]) {
     shape[12] = e->field_tma;
     shape[13] = e->cutoff ? e->nbl_row_cap : 0;
     shape[14] = e->cutoff ? e->nbl_cells : 0;
+    shape[15] = e->step_pdl;
     return ISSPA_OK;
 }
 
@@ -1636,21 +1643,33 @@ int isspa_autotune(isspa_engine *e, int reps, int shape[ISSPA_SHAPE_COUNT]) {
         // timed as single-step graph replays; positions, velocities and the
         // step counter are restored afterwards
         ck(cudaMemsetAsync(e->facc, 0, 3 * sizeof(unsigned long long) * e->n_atoms, e->stream));
-        if (e->opt.integrator == 0 && e->n_atoms > 0) {
+        if ((e->opt.integrator == 0 || e->opt.step_pdl == 0) && e->n_atoms > 0) {
             std::vector<float4> p0(e->n_atoms), v0(e->n_atoms);
             uint32_t st0 = 0;
             ck(cudaMemcpyAsync(p0.data(), e->pos, sizeof(float4) * e->n_atoms, cudaMemcpyDeviceToHost, e->stream));
             ck(cudaMemcpyAsync(v0.data(), e->vel, sizeof(float4) * e->n_atoms, cudaMemcpyDeviceToHost, e->stream));
             ck(cudaMemcpyAsync(&st0, e->d_step, sizeof(uint32_t), cudaMemcpyDeviceToHost, e->stream));
             ck(cudaStreamSynchronize(e->stream));
-            // three interleaved rounds, the minimum per mode: the modes differ
-            // by a few per cent where they differ at all
-            float t[4] = {0.f, 1e30f, 1e30f, 1e30f};
+            // candidates: the integrators (1, 2, 3) the options leave open, each
+            // with and without programmatic launches of the step chain (none in
+            // the single-kernel step); three interleaved rounds, the minimum
+            // per candidate: they differ by a few per cent where they differ
+            std::vector<std::pair<int, int>> cand;
+            for (int m : {1, 2, 3}) {
+                if (e->opt.integrator != 0 && m != e->integrator) continue;
+                if (m == 3 && !e->step_kernel_ok()) continue;
+                for (int pdl : {0, 1}) {
+                    if (m == 3 && pdl) continue;
+                    if (e->opt.step_pdl != 0 && pdl != (e->opt.step_pdl == 1 ? 1 : 0) && m != 3) continue;
+                    cand.emplace_back(m, pdl);
+                }
+            }
+            std::vector<float> t(cand.size(), 1e30f);
             int rounds = 3;
             for (int round = 0; round < rounds; ++round)
-                for (int m : {1, 2, 3}) {
-                    if (m == 3 && !e->step_kernel_ok()) continue;
-                    e->set_integrator(m);
+                for (size_t c = 0; c < cand.size(); ++c) {
+                    e->set_integrator(cand[c].first);
+                    e->step_pdl = cand[c].second;
                     e->invalidate_graphs();
                     cudaGraphExec_t g = e->capture(1);
                     auto one = [&] { ck(cudaGraphLaunch(g, e->stream)); };
@@ -1658,14 +1677,15 @@ int isspa_autotune(isspa_engine *e, int reps, int shape[ISSPA_SHAPE_COUNT]) {
                     if (first > 2.0f) rounds = 1;  // long steps: one round is enough
                     const int saved = reps;
                     reps = first > 2.0f ? saved : std::max(saved, 50);
-                    t[m] = std::min(t[m], time_it(one));
+                    t[c] = std::min(t[c], time_it(one));
                     reps = saved;
                     cudaGraphExecDestroy(g);
                 }
-            int best_m = 1;
-            for (int m : {2, 3})
-                if (t[m] < t[best_m]) best_m = m;
-            e->set_integrator(best_m);
+            size_t best = 0;
+            for (size_t c = 1; c < cand.size(); ++c)
+                if (t[c] < t[best]) best = c;
+            e->set_integrator(cand[best].first);
+            e->step_pdl = cand[best].second;
             ck(cudaMemcpyAsync(e->pos, p0.data(), sizeof(float4) * e->n_atoms, cudaMemcpyHostToDevice, e->stream));
             ck(cudaMemcpyAsync(e->vel, v0.data(), sizeof(float4) * e->n_atoms, cudaMemcpyHostToDevice, e->stream));
             ck(cudaMemcpyAsync(e->d_step, &st0, sizeof(uint32_t), cudaMemcpyHostToDevice, e->stream));

@@ -410,6 +410,8 @@ __device__ __forceinline__ void field_tile(const FieldArgs &a, int tile_index) {
 
 template <int S, bool GEN, bool RAW, bool VOTE, bool TMA = false>
 __global__ void __launch_bounds__(FieldShape<S>::kThreads) field_kernel(FieldArgs a) {
+    pdl_wait();
+    pdl_trigger();
     field_tile<S, GEN, RAW, VOTE, TMA>(a, blockIdx.x);
 }
 
@@ -583,6 +585,8 @@ __device__ __forceinline__ void force_item(const ForceArgs &a, int item_index) {
 template <bool LJ, int A, bool VOTE = false>
 __global__ void __launch_bounds__(ForceShape<A>::kThreads, VOTE ? 8 : ForceShape<A>::kMinBlocks)
     force_kernel(ForceArgs a) {
+    pdl_wait();
+    pdl_trigger();
     force_item<LJ, A, VOTE>(a, blockIdx.x);
 }
 
@@ -618,7 +622,7 @@ __global__ void __launch_bounds__(kFieldThreads, 4) step_kernel(StepArgs a) {
 
 template <int S, bool GEN, bool RAW, bool VOTE = false, bool TMA = false>
 void launch_field_t(const FieldArgs &a, cudaStream_t s) {
-    field_kernel<S, GEN, RAW, VOTE, TMA><<<a.n_tiles, FieldShape<S>::kThreads, 0, s>>>(a);
+    launch_chain(field_kernel<S, GEN, RAW, VOTE, TMA>, a.n_tiles, FieldShape<S>::kThreads, s, a);
 }
 
 template <int S>
@@ -714,14 +718,14 @@ cudaError_t launch_step(const StepArgs &a, int grid, cudaStream_t s) {
 void launch_force(const ForceArgs &a, cudaStream_t s) {
     if (a.n_items <= 0) return;
     if (a.vote && a.atoms_per_thread != 2) {
-        if (a.terms & 2) force_kernel<true, 1, true><<<a.n_items, ForceShape<1>::kThreads, 0, s>>>(a);
-        else force_kernel<false, 1, true><<<a.n_items, ForceShape<1>::kThreads, 0, s>>>(a);
+        if (a.terms & 2) launch_chain(force_kernel<true, 1, true>, a.n_items, ForceShape<1>::kThreads, s, a);
+        else launch_chain(force_kernel<false, 1, true>, a.n_items, ForceShape<1>::kThreads, s, a);
     } else if (a.atoms_per_thread == 2) {
-        if (a.terms & 2) force_kernel<true, 2><<<a.n_items, ForceShape<2>::kThreads, 0, s>>>(a);
-        else force_kernel<false, 2><<<a.n_items, ForceShape<2>::kThreads, 0, s>>>(a);
+        if (a.terms & 2) launch_chain(force_kernel<true, 2>, a.n_items, ForceShape<2>::kThreads, s, a);
+        else launch_chain(force_kernel<false, 2>, a.n_items, ForceShape<2>::kThreads, s, a);
     } else {
-        if (a.terms & 2) force_kernel<true, 1><<<a.n_items, ForceShape<1>::kThreads, 0, s>>>(a);
-        else force_kernel<false, 1><<<a.n_items, ForceShape<1>::kThreads, 0, s>>>(a);
+        if (a.terms & 2) launch_chain(force_kernel<true, 1>, a.n_items, ForceShape<1>::kThreads, s, a);
+        else launch_chain(force_kernel<false, 1>, a.n_items, ForceShape<1>::kThreads, s, a);
     }
 }
 

@@ -56,6 +56,8 @@ __global__ void __launch_bounds__(kUsThreads) umbrella_kernel(UmbrellaArgs a) {
 // Every block reads the step counter first; the last block to finish
 // advances it (no block waits on another).
 __global__ void leapfrog_kernel(LeapfrogArgs a) {
+    pdl_wait();
+    pdl_trigger();
     const uint32_t step = *a.step_ptr;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < a.n_atoms) leapfrog_atom(a, i, step, nullptr);
@@ -216,8 +218,15 @@ cudaError_t launch_integrator(const IntegratorArgs &a, int grid, cudaStream_t s)
     return cudaLaunchKernelEx(&cfg, integrator_kernel, a);
 }
 
+namespace {
+thread_local bool t_chain_pdl = false;
+}
+bool chain_pdl() { return t_chain_pdl; }
+PdlScope::PdlScope(bool on) : prev_(t_chain_pdl) { t_chain_pdl = on; }
+PdlScope::~PdlScope() { t_chain_pdl = prev_; }
+
 void launch_leapfrog(const LeapfrogArgs &a, cudaStream_t s) {
-    if (a.n_atoms > 0) leapfrog_kernel<<<(a.n_atoms + 127) / 128, 128, 0, s>>>(a);
+    if (a.n_atoms > 0) launch_chain(leapfrog_kernel, (a.n_atoms + 127) / 128, 128, s, a);
 }
 
 void launch_neighbor_list(const ListArgs &a, cudaStream_t s) {

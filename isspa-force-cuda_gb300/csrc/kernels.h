@@ -244,6 +244,43 @@ void launch_nonbond_energy(const NonbondArgs &a, double *energy, cudaStream_t s)
 void launch_bonded_energy(const BondedArgs &a, double *energy, cudaStream_t s);
 void launch_state_energy(const StateEnergyArgs &a, double *energy, cudaStream_t s);
 
+// ---- the step's main chain: field -> force -> leapfrog ---------------------
+// While a PdlScope lives on a thread, the chain's kernels (each opens with
+// pdl_wait) are launched from that thread as programmatic dependents of the
+// kernel before them on the stream: a kernel's launch and block scheduling
+// overlap the tail of the one it depends on.  Every other kernel, and the
+// chain outside such a scope, launches as an ordinary kernel.
+bool chain_pdl();
+class PdlScope {
+  public:
+    explicit PdlScope(bool on);
+    ~PdlScope();
+    PdlScope(const PdlScope &) = delete;
+    PdlScope &operator=(const PdlScope &) = delete;
+
+  private:
+    bool prev_;
+};
+#ifdef __CUDACC__
+template <class... P, class... A>
+inline void launch_chain(void (*k)(P...), unsigned grid, unsigned block, cudaStream_t s, const A &...args) {
+    if (!chain_pdl()) {
+        k<<<grid, block, 0, s>>>(args...);
+        return;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k, args...);  // a failure is the thread's last error
+}
+#endif
+
 void launch_adjoint(const AdjointArgs &a, cudaStream_t s);
 void launch_field(const FieldArgs &a, int split, bool raw, cudaStream_t s);
 void launch_force(const ForceArgs &a, cudaStream_t s);

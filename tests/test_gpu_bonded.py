@@ -15,6 +15,10 @@
 * The single-kernel step (field, nonbond, bonded | force | update in one
   cooperative kernel) gives the separate kernels' trajectory bit for bit with
   the same launch shapes, on the same three systems.
+* The step chain (field, force, leapfrog) launched as programmatic
+  dependents gives the ordinary launches' trajectory bit for bit, with
+  either integrator, through graph replays, direct stream launches and
+  isspa_step_host with device-mapped buffers.
 * The autotuner's integrator choice leaves the state where it was.
 * The grid barrier's bounded wait: a barrier left mid-count runs out,
   the step reports ISSPA_ERR_TIMEOUT without a fault, and the same engine
@@ -179,6 +183,49 @@ def test_single_kernel_step_bit_identical(which, adi2):
     assert np.array_equal(c1[0], c3[0]) and np.array_equal(c1[1], c3[1])
 
 
+@pytest.mark.parametrize("integ", [1, 2])
+@pytest.mark.parametrize("which", ["medium", "batched-umbrella", "adi2-umbrella"])
+def test_programmatic_launches_bit_identical(which, integ, adi2):
+    wins = _windows(which, adi2)
+    runs = {}
+    for pdl in (2, 1):
+        for graph in (True, False):
+            eng = ig.Engine(wins, integrator=integ, step_pdl=pdl, use_graph=graph)
+            sh = eng.shapes()
+            assert sh["integrator"] == integ and sh["step_pdl"] == (1 if pdl == 1 else 0)
+            eng.step(12)
+            runs[(pdl, graph)] = (eng.positions(), eng.velocities(), eng.get_step(), eng.device_status())
+            eng.close()
+    # isspa_step_host, device-mapped buffers read and written by the kernels
+    eng = ig.Engine(wins, integrator=integ, step_pdl=1)
+    n = eng.n_atoms
+    bufs = [ig.host_array((n, 4)) for _ in range(5)]
+    bufs[0][:] = eng.positions()
+    bufs[1][:] = eng.velocities()
+    for k in range(12):
+        src, dst = (0, 2) if k % 2 == 0 else (2, 0)
+        eng.step_host(bufs[src], bufs[src + 1], bufs[dst], bufs[dst + 1], bufs[4])
+    runs["host"] = (bufs[0].copy(), bufs[1].copy(), eng.get_step(), eng.device_status())
+    eng.close()
+    p0, v0, st0, ds0 = runs[(2, True)]
+    assert ds0 == 0 and st0 == 12
+    for key, (p, v, st, ds) in runs.items():
+        assert ds == 0 and st == 12, key
+        assert np.array_equal(p, p0), key
+        assert np.array_equal(v, v0), key
+
+
+def test_step_pdl_option_checked():
+    s = ig.synth.config_small(seed=1)
+    for bad in (-1, 3):
+        with pytest.raises(RuntimeError):
+            ig.Engine(s, step_pdl=bad)
+    eng = ig.Engine(s, integrator=3, step_pdl=1)
+    assert eng.shapes()["integrator"] == 3  # the single-kernel step has no chain to launch
+    eng.step(2)
+    assert eng.device_status() == 0
+
+
 def test_autotune_restores_state():
     s = ig.synth.config_small(seed=1)
     a = ig.Engine(s)
@@ -186,7 +233,7 @@ def test_autotune_restores_state():
     a.step(3)
     b.step(3)
     sh = a.autotune()
-    assert sh["integrator"] in (1, 2, 3)
+    assert sh["integrator"] in (1, 2, 3) and sh["step_pdl"] in (0, 1)
     assert a.get_step() == 3
     assert np.array_equal(a.positions(), b.positions())
     assert np.array_equal(a.velocities(), b.velocities())
