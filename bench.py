@@ -699,7 +699,8 @@ def run_profile_case(args):
                         force_atoms_per_thread=fixed["force_atoms_per_thread"],
                         force_tail_chunk=fixed["force_tail_chunk"], field_vote=fixed["field_vote"],
                         force_vote=fixed["force_vote"], integrator=fixed["integrator"],
-                        nonbond_chunk=fixed["nonbond_partners_per_item"], field_tma=fixed["field_tma"])
+                        nonbond_chunk=fixed["nonbond_partners_per_item"], field_tma=fixed["field_tma"],
+                        step_pdl=1 if fixed.setdefault("step_pdl", 0) else 2)
         shapes = eng.shapes()
         if shapes != fixed:
             raise RuntimeError(f"shapes from {args.shapes_file} not reproduced: {shapes} != {fixed}")
