@@ -622,9 +622,10 @@ struct isspa_engine {
         }
         return false;
     }
-    // Step with the two independent chains (field->force and bonded, umbrella,
-    // nonbond) on forked streams; both add into the same accumulator.  With
-    // `timed`, CUDA events bracket every kernel on the stream it runs on.
+    // Step with three independent chains (field -> force; bonded -> umbrella;
+    // nonbond) on forked streams, all adding into the same accumulator, joined
+    // before the update.  With `timed`, CUDA events bracket every kernel on
+    // the stream it runs on.
     void enqueue_step_forked(bool timed = false) {
         // External event-record nodes: a plain cudaEventRecord under capture only
         // orders the graph and is never recorded at replay time.
