@@ -54,7 +54,8 @@ __global__ void __launch_bounds__(kUsThreads) umbrella_kernel(UmbrellaArgs a) {
 }
 
 // Every block reads the step counter first; the last block to finish
-// advances it (no block waits on another).
+// advances it (no block waits on another).  A single block advances it after
+// its own barrier, without the completion count.
 __global__ void leapfrog_kernel(LeapfrogArgs a) {
     pdl_wait();
     pdl_trigger();
@@ -62,6 +63,10 @@ __global__ void leapfrog_kernel(LeapfrogArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < a.n_atoms) leapfrog_atom(a, i, step, nullptr);
     __syncthreads();
+    if (gridDim.x == 1) {
+        if (threadIdx.x == 0) *a.step_ptr = step + 1u;
+        return;
+    }
     if (threadIdx.x == 0) {
         __threadfence();
         const unsigned int prev = atomicAdd(a.done_ptr, 1u);

@@ -5,6 +5,7 @@
 #pragma once
 #include <climits>
 #include <cuda_runtime.h>
+#include <type_traits>
 
 #include "kernels.h"
 #include "philox.h"
@@ -84,13 +85,18 @@ __device__ __forceinline__ void nonbond_item(const NonbondArgs &a, int item_inde
             s_t[t] = ty.x;
         }
         __syncthreads();
-        // the pair (i, staged partner k); EX: excluded (IS-SPA correction only)
-        auto pair = [&](int k, bool ex) {
+        // the pair (i, staged partner k); EX: excluded (IS-SPA correction
+        // only).  MASKED: the exclusion bit and the self pair are applied by
+        // selects instead of branches (the self pair gets d2 = 1 and adds
+        // nothing), so a group with exclusions keeps an unrolled loop; the
+        // values are those of the branching form.
+        auto pair_t = [&](int k, bool ex, bool self, auto masked) {
+            constexpr bool MASKED = decltype(masked)::value;
             const float4 xj = s_x[k];
             const float rx = mimg(xi.x - xj.x, L, h);
             const float ry = mimg(xi.y - xj.y, L, h);
             const float rz = mimg(xi.z - xj.z, L, h);
-            const float d2 = dist2f(rx, ry, rz);
+            const float d2 = MASKED && self ? 1.0f : dist2f(rx, ry, rz);
             const float ri = rsqrtf(d2);
             const float ri2 = ri * ri;
             const float qq = xi.w * xj.w;
@@ -99,18 +105,22 @@ __device__ __forceinline__ void nonbond_item(const NonbondArgs &a, int item_inde
                 const float4 c = s_c[k];
                 fs = d2 > c.y ? kfar * qq * ri2 * ri : -qq * c.w * (c.z - 3.0f * d2 * ri);
             }
-            if (!ex) {
+            if (MASKED || !ex) {
+                float fp = fs;
                 if (terms & 1) {  // LJ (:131-132)
                     const float2 ab = SMEM_AB ? s_ab[trow + s_t[k]] : __ldg(a.ljab + trow + s_t[k]);
                     const float r6 = ri2 * ri2 * ri2;
-                    fs += r6 * fmaf(12.0f * ab.x, r6, -6.0f * ab.y) * ri2;
+                    fp += r6 * fmaf(12.0f * ab.x, r6, -6.0f * ab.y) * ri2;
                 }
-                if (terms & 2) fs += qq * ri2 * ri;  // Coulomb (:136)
+                if (terms & 2) fp += qq * ri2 * ri;  // Coulomb (:136)
+                fs = MASKED && ex ? fs : fp;
             }
+            if (MASKED) fs = self ? 0.0f : fs;
             ax = fmaf(fs, rx, ax);
             ay = fmaf(fs, ry, ay);
             az = fmaf(fs, rz, az);
         };
+        auto pair = [&](int k, bool ex) { pair_t(k, ex, false, std::false_type{}); };
 #pragma unroll
         for (int q = 0; q < kNbThreads / 32; ++q) {
             const int k0 = 32 * q;
@@ -118,11 +128,17 @@ __device__ __forceinline__ void nonbond_item(const NonbondArgs &a, int item_inde
             const int kn = min(32, jn - k0);
             const unsigned mq = m[q];
             if (__any_sync(0xffffffffu, mq != 0u)) {
+                // exclusions or the self pair in this group: masked pairs,
+                // unrolled like the unmasked group below
+                const int self_k = i - (jb + k0);  // the self pair's k, if in this group
+                if (kn == 32) {
+#pragma unroll 4
+                    for (int k = 0; k < 32; ++k)
+                        pair_t(k0 + k, (mq >> k) & 1u, k == self_k, std::true_type{});
+                } else {
 #pragma unroll 1
-                for (int k = 0; k < kn; ++k) {
-                    const bool bit = (mq >> k) & 1u;
-                    if (bit && jb + k0 + k == i) continue;
-                    pair(k0 + k, bit);
+                    for (int k = 0; k < kn; ++k)
+                        pair_t(k0 + k, (mq >> k) & 1u, k == self_k, std::true_type{});
                 }
             } else if (kn == 32) {
 #pragma unroll 8
