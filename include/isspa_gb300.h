@@ -158,6 +158,14 @@ typedef struct isspa_engine_options {
                               access, so its launch overlaps the other's tail; same results);
                               2: ordinary launches; 0 => 2 until isspa_autotune times both and
                               keeps the faster.  The single-kernel step has no chain */
+    int isspa_fused;       /* 1: the field and force passes run as one launch over the field
+                              tiles: each block computes its points' fields, then those points'
+                              forces on every atom of its window (for small windows; needs
+                              Philox points, the tabulated LJ term and a field split of 4, 8 or
+                              16, else the separate passes run).  Forces equal the separate
+                              passes' up to FP32 summation order.  2: separate passes; 0 => 2
+                              until isspa_autotune times both (windows of up to 1024 atoms)
+                              and keeps the faster */
 } isspa_engine_options;
 
 #define ISSPA_TERMS_NONE (-1)
@@ -225,8 +233,9 @@ int isspa_engine_info(const isspa_engine *e, int *n_windows, int *n_atoms_total,
  * [12] 1 when the field pass stages its atoms by bulk copies (TMA), [13] in
  * cutoff mode the partners a neighbour-list row holds (0 otherwise), [14] in
  * cutoff mode the cells of all windows' cell grids (0 otherwise), [15] 1 when
- * isspa_step launches its kernel chain as programmatic dependents. */
-#define ISSPA_SHAPE_COUNT 16
+ * isspa_step launches its kernel chain as programmatic dependents, [16] 1 when
+ * the field and force passes run as one fused launch. */
+#define ISSPA_SHAPE_COUNT 17
 int isspa_engine_shapes(const isspa_engine *e, int shape[ISSPA_SHAPE_COUNT]);
 /* Autotuner: times every field-pass atom split (per-pair and warp-voted
  * loops, atoms staged by loads or by bulk copies) and, for 1 and 2 receiving
@@ -236,10 +245,11 @@ int isspa_engine_shapes(const isspa_engine *e, int shape[ISSPA_SHAPE_COUNT]);
  * chosen list) on this engine's own
  * workload with CUDA events (reps launches each), keeps the fastest of each
  * and reports the result as isspa_engine_shapes does.  When the options leave
- * the integrator or step_pdl open (0), it then times single-step graph
- * replays of the open choices (separate kernels, fused integrator,
- * single-kernel step; with and without programmatic launches) and keeps the
- * fastest (the nonbond partners per item are timed too); positions,
+ * the integrator, step_pdl or isspa_fused open (0), it then times single-step
+ * graph replays of the open choices (separate kernels, fused integrator,
+ * single-kernel step; with and without programmatic launches; with and
+ * without the fused field + force launch) and keeps the fastest (the nonbond
+ * partners per item are timed too); positions,
  * velocities and the step counter are restored.  Clears the force
  * accumulator; invalidates captured graphs. */
 int isspa_autotune(isspa_engine *e, int reps, int shape[ISSPA_SHAPE_COUNT]);

@@ -92,6 +92,7 @@ struct isspa_engine {
     int field_vote = 0;  // field pass in warp-voted groups of four atoms
     int field_tma = 0;   // field pass stages its atom rounds by 1-D bulk copies (TMA)
     int step_pdl = 0;    // step chain launched as programmatic dependents (1) or not (0)
+    int isspa_fused = 0;  // field and force passes as one launch (1) when fused_ok()
     int force_vote = 0;  // force pass in warp-voted groups of four points (1 atom per thread)
     int force_apt = 1;  // receiving atoms per force-kernel thread (1 or 2)
     // step integrator: 1 = bonded, umbrella and leapfrog kernels (bonded and
@@ -595,8 +596,27 @@ struct isspa_engine {
         integrator = m;
     }
 
+    // The fused field + force launch needs Philox points, the tabulated LJ term
+    // and a field split of 4, 8 or 16; it is offered for windows of at most
+    // kFusedMaxAtoms atoms (its force phase adds one set of atomics per atom
+    // and field tile).
+    static constexpr int kFusedMaxAtoms = 1024;
+    int max_window_atoms() const {
+        int m = 0;
+        for (const WinDev &d : win_h) m = std::max(m, d.n_atoms);
+        return m;
+    }
+    bool fused_ok() const {
+        return !inject && (opt.isspa_terms & 2) && field_force_fusable(field_split) && n_field_tiles > 0;
+    }
+    bool fused() const { return isspa_fused == 1 && fused_ok(); }
+
     // ---------------------------------------------------------- sequences
     void enqueue_isspa(cudaStream_t s, bool raw = false) {
+        if (!raw && fused()) {
+            launch_field_force(field_args(), force_args(), field_split, s);
+            return;
+        }
         launch_field(field_args(), field_split, raw, s);
         launch_force(force_args(), s);
     }
@@ -612,7 +632,7 @@ struct isspa_engine {
         const bool one = integrator == 3;
         switch (k) {
             case ISSPA_K_FIELD: return !one && opt.isspa_terms && n_field_tiles > 0;
-            case ISSPA_K_FORCE: return !one && opt.isspa_terms && n_force_items > 0;
+            case ISSPA_K_FORCE: return !one && !fused() && opt.isspa_terms && n_force_items > 0;
             case ISSPA_K_NONBOND: return !one && opt.nonbond_terms && (cutoff ? n_atoms > 0 : n_nb_items > 0);
             case ISSPA_K_STEP: return one && n_atoms > 0;
             case ISSPA_K_BONDED: return integrator == 1 && n_bonds + n_angles + n_dihs > 0;
@@ -645,11 +665,16 @@ struct isspa_engine {
         ck(cudaStreamWaitEvent(side, ev_fork, 0));
         ck(cudaStreamWaitEvent(side2, ev_fork, 0));
         mark(ISSPA_K_FIELD, 0, stream);
-        launch_field(field_args(), field_split, false, stream);
-        mark(ISSPA_K_FIELD, 1, stream);
-        mark(ISSPA_K_FORCE, 0, stream);
-        launch_force(force_args(), stream);
-        mark(ISSPA_K_FORCE, 1, stream);
+        if (fused()) {  // one launch for both passes; timed as the field kernel
+            launch_field_force(field_args(), force_args(), field_split, stream);
+            mark(ISSPA_K_FIELD, 1, stream);
+        } else {
+            launch_field(field_args(), field_split, false, stream);
+            mark(ISSPA_K_FIELD, 1, stream);
+            mark(ISSPA_K_FORCE, 0, stream);
+            launch_force(force_args(), stream);
+            mark(ISSPA_K_FORCE, 1, stream);
+        }
         if (integrator == 1) {
             mark(ISSPA_K_BONDED, 0, side);
             launch_bonded(bonded_args(1, 1, 1), side);
@@ -975,6 +1000,7 @@ void build(isspa_engine &E, const std::vector<isspa_host_system> &ws) {
     E.field_vote = E.opt.field_vote == 1 ? 1 : 0;
     E.field_tma = E.opt.field_tma == 1 ? 1 : 0;
     E.step_pdl = E.opt.step_pdl == 1 ? 1 : 0;
+    E.isspa_fused = E.opt.isspa_fused == 1 ? 1 : 0;
     E.force_vote = E.opt.force_vote == 1 ? 1 : 0;
     E.force_apt = E.opt.force_atoms_per_thread == 2 ? 2 : 1;
     E.set_force_chunk(E.opt.force_chunk > 0 ? E.opt.force_chunk : E.default_force_chunk(),
@@ -1237,7 +1263,7 @@ int isspa_engine_create(const isspa_system_desc *windows, int n_windows, const i
     else if (e->opt.nonbond_terms == 0) e->opt.nonbond_terms = 7;
     if (!(e->opt.nonbond_cutoff >= 0.f) || !(e->opt.nonbond_skin >= 0.f) || e->opt.nonbond_list_max < 0 ||
         std::isinf(e->opt.nonbond_cutoff) || std::isinf(e->opt.nonbond_skin) || e->opt.step_pdl < 0 ||
-        e->opt.step_pdl > 2)
+        e->opt.step_pdl > 2 || e->opt.isspa_fused < 0 || e->opt.isspa_fused > 2)
         return ISSPA_ERR_ARG;
     if (cudaGetDevice(&e->device) != cudaSuccess) {
         cudaGetLastError();
@@ -1296,6 +1322,7 @@ int isspa_engine_shapes(const isspa_engine *e, int shape[ISSPA_SHAPE_COUNT]) {
     shape[13] = e->cutoff ? e->nbl_row_cap : 0;
     shape[14] = e->cutoff ? e->nbl_cells : 0;
     shape[15] = e->step_pdl;
+    shape[16] = e->fused() ? 1 : 0;
     return ISSPA_OK;
 }
 
@@ -1644,7 +1671,8 @@ int isspa_autotune(isspa_engine *e, int reps, int shape[ISSPA_SHAPE_COUNT]) {
         // timed as single-step graph replays; positions, velocities and the
         // step counter are restored afterwards
         ck(cudaMemsetAsync(e->facc, 0, 3 * sizeof(unsigned long long) * e->n_atoms, e->stream));
-        if ((e->opt.integrator == 0 || e->opt.step_pdl == 0) && e->n_atoms > 0) {
+        const bool try_fused = e->opt.isspa_fused == 0 && e->fused_ok() && e->max_window_atoms() <= isspa_engine::kFusedMaxAtoms;
+        if ((e->opt.integrator == 0 || e->opt.step_pdl == 0 || try_fused) && e->n_atoms > 0) {
             std::vector<float4> p0(e->n_atoms), v0(e->n_atoms);
             uint32_t st0 = 0;
             ck(cudaMemcpyAsync(p0.data(), e->pos, sizeof(float4) * e->n_atoms, cudaMemcpyDeviceToHost, e->stream));
@@ -1652,25 +1680,33 @@ int isspa_autotune(isspa_engine *e, int reps, int shape[ISSPA_SHAPE_COUNT]) {
             ck(cudaMemcpyAsync(&st0, e->d_step, sizeof(uint32_t), cudaMemcpyDeviceToHost, e->stream));
             ck(cudaStreamSynchronize(e->stream));
             // candidates: the integrators (1, 2, 3) the options leave open, each
-            // with and without programmatic launches of the step chain (none in
-            // the single-kernel step); three interleaved rounds, the minimum
-            // per candidate: they differ by a few per cent where they differ
-            std::vector<std::pair<int, int>> cand;
+            // with and without programmatic launches of the step chain and, for
+            // small windows, with the fused field + force launch (neither in the
+            // single-kernel step); three interleaved rounds, the minimum per
+            // candidate: they differ by a few per cent where they differ
+            struct Cand {
+                int m, pdl, fused;
+            };
+            std::vector<Cand> cand;
+            const int fixed_fused = e->isspa_fused;
             for (int m : {1, 2, 3}) {
                 if (e->opt.integrator != 0 && m != e->integrator) continue;
                 if (m == 3 && !e->step_kernel_ok()) continue;
-                for (int pdl : {0, 1}) {
-                    if (m == 3 && pdl) continue;
-                    if (e->opt.step_pdl != 0 && pdl != (e->opt.step_pdl == 1 ? 1 : 0) && m != 3) continue;
-                    cand.emplace_back(m, pdl);
-                }
+                for (int pdl : {0, 1})
+                    for (int fu : {0, 1}) {
+                        if (m == 3 && (pdl || fu)) continue;
+                        if (e->opt.step_pdl != 0 && m != 3 && pdl != (e->opt.step_pdl == 1 ? 1 : 0)) continue;
+                        if (m != 3 && (try_fused ? false : fu != fixed_fused)) continue;
+                        cand.push_back({m, pdl, fu});
+                    }
             }
             std::vector<float> t(cand.size(), 1e30f);
             int rounds = 3;
             for (int round = 0; round < rounds; ++round)
                 for (size_t c = 0; c < cand.size(); ++c) {
-                    e->set_integrator(cand[c].first);
-                    e->step_pdl = cand[c].second;
+                    e->set_integrator(cand[c].m);
+                    e->step_pdl = cand[c].pdl;
+                    e->isspa_fused = cand[c].fused;
                     e->invalidate_graphs();
                     cudaGraphExec_t g = e->capture(1);
                     auto one = [&] { ck(cudaGraphLaunch(g, e->stream)); };
@@ -1685,8 +1721,9 @@ int isspa_autotune(isspa_engine *e, int reps, int shape[ISSPA_SHAPE_COUNT]) {
             size_t best = 0;
             for (size_t c = 1; c < cand.size(); ++c)
                 if (t[c] < t[best]) best = c;
-            e->set_integrator(cand[best].first);
-            e->step_pdl = cand[best].second;
+            e->set_integrator(cand[best].m);
+            e->step_pdl = cand[best].pdl;
+            e->isspa_fused = cand[best].fused;
             ck(cudaMemcpyAsync(e->pos, p0.data(), sizeof(float4) * e->n_atoms, cudaMemcpyHostToDevice, e->stream));
             ck(cudaMemcpyAsync(e->vel, v0.data(), sizeof(float4) * e->n_atoms, cudaMemcpyHostToDevice, e->stream));
             ck(cudaMemcpyAsync(e->d_step, &st0, sizeof(uint32_t), cudaMemcpyHostToDevice, e->stream));

@@ -117,6 +117,12 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned pari
     }
 }
 
+// One MC point's records side by side in shared memory: a single base address
+// per point, the five float4 at immediate offsets (q3 / q4 picked per lane).
+struct alignas(16) PointRec {
+    float4 q[5];
+};
+
 // Block shape of the field kernel: S warps split the atom loop of each group
 // of 32 points; 4 warps per block up to S = 4, then 32*S threads.
 template <int S>
@@ -132,8 +138,12 @@ struct FieldShape {
 // at use (the same products, so the same results).  One warp vote per round
 // makes a bounded wait that gave up block-uniform: the block then flags
 // kStatusTimeout, waits (bounded) for its copies still in flight and exits.
-template <int S, bool GEN, bool RAW, bool VOTE, bool TMA = false>
-__device__ __forceinline__ void field_tile(const FieldArgs &a, int tile_index) {
+// FUSE: the tile's point records are also left in s_rec[slot] for a force
+// phase of the same block (which follows a barrier after this function; no
+// barrier of this function comes after a thread's early return).
+template <int S, bool GEN, bool RAW, bool VOTE, bool TMA = false, bool FUSE = false>
+__device__ __forceinline__ void field_tile(const FieldArgs &a, int tile_index, PointRec *s_rec = nullptr) {
+    static_assert(!FUSE || (GEN && !RAW && !TMA), "the fused pass draws its points and stages by loads");
     constexpr int kT = FieldShape<S>::kThreads;
     // atoms staged per round: four per thread below a split of 4, so the
     // warps' compute phases between barriers are four times longer (64 windows
@@ -401,11 +411,23 @@ __device__ __forceinline__ void field_tile(const FieldArgs &a, int tile_index) {
     const float a3 = mp ? kO0 * p3 * sden : 0.0f;
     const float hx = ex * im, hy = ey * im, hz = ez * im;
     const float cd = cdd ? kP0 * inv_n * (1.0f / 3.0f) : 0.0f;  // p0 E0 / (3 n)
-    a.out.q0[pg] = make_float4(px, py, pz, sden);
-    a.out.q1[pg] = make_float4(hx, hy, hz, 1.5f * a2);
-    a.out.q2[pg] = make_float4(7.5f * a2, 17.5f * a3, 3.0f * a2, 7.5f * a3);
-    a.out.q3[pg] = make_float4(a1 * hx, a1 * hy, a1 * hz, 1.5f * a3);
-    a.out.q4[pg] = make_float4(fmaf(a1, hx, cd * fx), fmaf(a1, hy, cd * fy), fmaf(a1, hz, cd * fz), 1.5f * a3);
+    const float4 r0 = make_float4(px, py, pz, sden);
+    const float4 r1 = make_float4(hx, hy, hz, 1.5f * a2);
+    const float4 r2 = make_float4(7.5f * a2, 17.5f * a3, 3.0f * a2, 7.5f * a3);
+    const float4 r3 = make_float4(a1 * hx, a1 * hy, a1 * hz, 1.5f * a3);
+    const float4 r4 = make_float4(fmaf(a1, hx, cd * fx), fmaf(a1, hy, cd * fy), fmaf(a1, hz, cd * fz), 1.5f * a3);
+    a.out.q0[pg] = r0;
+    a.out.q1[pg] = r1;
+    a.out.q2[pg] = r2;
+    a.out.q3[pg] = r3;
+    a.out.q4[pg] = r4;
+    if (FUSE) {
+        s_rec[slot].q[0] = r0;
+        s_rec[slot].q[1] = r1;
+        s_rec[slot].q[2] = r2;
+        s_rec[slot].q[3] = r3;
+        s_rec[slot].q[4] = r4;
+    }
 }
 
 template <int S, bool GEN, bool RAW, bool VOTE, bool TMA = false>
@@ -414,12 +436,6 @@ __global__ void __launch_bounds__(FieldShape<S>::kThreads) field_kernel(FieldArg
     pdl_trigger();
     field_tile<S, GEN, RAW, VOTE, TMA>(a, blockIdx.x);
 }
-
-// One MC point's records side by side in shared memory: a single base address
-// per point, the five float4 at immediate offsets (q3 / q4 picked per lane).
-struct alignas(16) PointRec {
-    float4 q[5];
-};
 
 // LJ = include the tabulated mean LJ force (term bit 2); the multipole and CDD
 // terms are shaped by the per-point constants of the field pass.  A = receiving
@@ -431,6 +447,48 @@ struct ForceShape {
     static constexpr int kThreads = kForceThreads / A;
     static constexpr int kMinBlocks = A == 1 ? 10 : 12;  // 48 / 85 registers per thread
 };
+
+// One MC point's force terms on a receiving atom, r = point - atom (minimum
+// image) and d2 = |r|^2: the multipole terms (:274-289, with the CDD term
+// (:306-312) folded into the record D) into q per unit -q_i vtot_i, the
+// tabulated mean LJ force (:291-305) into l per unit -vtot_i.  rm2 and frow
+// belong to the atom's type; FAR: the point is known to lie outside rmax.
+template <bool LJ, bool FAR>
+__device__ __forceinline__ void point_force(const float4 *R, float rx, float ry, float rz, float d2, float rm2,
+                                            int frow, const ForceArgs &a, float &qx, float &qy, float &qz,
+                                            float &lx, float &ly, float &lz) {
+    const float4 E = R[1];
+    const float4 K = R[2];
+    const bool inside = !FAR && d2 <= rm2;  // (:291)
+    const float ri = rsqrtf(d2);
+    const float ri2 = ri * ri;
+    const float ri3 = ri2 * ri;
+    const float ri5 = ri3 * ri2;
+    const float4 D = R[inside ? 3 : 4];
+    const float w = fmaf(E.x, rx, fmaf(E.y, ry, E.z * rz));
+    const float dD = fmaf(D.x, rx, fmaf(D.y, ry, D.z * rz));
+    const float g = w * ri2;
+    float X = (w * g) * fmaf(K.y, g, K.x);
+    X = fmaf(3.0f, dD, X) - E.w;
+    X = fmaf(-K.w, g, X);
+    const float cR = X * ri5;
+    const float cE = fmaf(-D.w, ri2, fmaf(K.w, g, K.z) * g) * ri3;
+    qx = fmaf(cR, rx, fmaf(-cE, E.x, fmaf(-ri3, D.x, qx)));
+    qy = fmaf(cR, ry, fmaf(-cE, E.y, fmaf(-ri3, D.y, qy)));
+    qz = fmaf(cR, rz, fmaf(-cE, E.z, fmaf(-ri3, D.z, qz)));
+    if (LJ && inside) {
+        const float dist = __fsqrt_rn(d2);
+        const int bin = (int)__fmaf_rn(__fsub_rn(dist, a.f_r0), a.f_inv, 0.5f);
+        if (bin >= 0 && bin < a.n_f) {
+            const float2 tv = __ldg(a.ftab + frow + bin);
+            const float fr = (dist - fmaf((float)bin, a.f_dr, a.f_r0)) * a.f_inv;
+            const float fv = fmaf(fr, tv.y - tv.x, tv.x) * R[0].w * ri;
+            lx = fmaf(fv, rx, lx);
+            ly = fmaf(fv, ry, ly);
+            lz = fmaf(fv, rz, lz);
+        }
+    }
+}
 
 // VOTE (one atom per thread only): points in groups of four with one warp
 // vote per group on "any lane has any of them inside rmax"; a group with none
@@ -447,7 +505,6 @@ __device__ __forceinline__ void force_item(const ForceArgs &a, int item_index) {
     const int2 ch = a.chunks[item.w];
     const int t = threadIdx.x;
     const float L = W.box, h = W.hbox;
-    const float f_r0 = a.f_r0, f_dr = a.f_dr, f_inv = a.f_inv;
     const int nf = a.n_f;
     bool active[A];
     int ai[A], frow[A];
@@ -492,40 +549,8 @@ __device__ __forceinline__ void force_item(const ForceArgs &a, int item_index) {
         // the pair (staged point k, receiving atom u) after its geometry; FAR:
         // the point is known to lie outside rmax of the atom's type
         auto pair = [&](int k, int u, float rx, float ry, float rz, float d2, auto far) {
-            constexpr bool FAR = decltype(far)::value;
-            const float4 *R = s_p[k].q;
-            const float4 E = R[1];
-            const float4 K = R[2];
-            const bool inside = !FAR && d2 <= rm2[u];  // (:291)
-            const float ri = rsqrtf(d2);
-            const float ri2 = ri * ri;
-            const float ri3 = ri2 * ri;
-            const float ri5 = ri3 * ri2;
-            const float4 D = R[inside ? 3 : 4];
-            // multipole (:274-289) with the CDD term (:306-312) folded into D
-            const float w = fmaf(E.x, rx, fmaf(E.y, ry, E.z * rz));
-            const float dD = fmaf(D.x, rx, fmaf(D.y, ry, D.z * rz));
-            const float g = w * ri2;
-            float X = (w * g) * fmaf(K.y, g, K.x);
-            X = fmaf(3.0f, dD, X) - E.w;
-            X = fmaf(-K.w, g, X);
-            const float cR = X * ri5;
-            const float cE = fmaf(-D.w, ri2, fmaf(K.w, g, K.z) * g) * ri3;
-            qx[u] = fmaf(cR, rx, fmaf(-cE, E.x, fmaf(-ri3, D.x, qx[u])));
-            qy[u] = fmaf(cR, ry, fmaf(-cE, E.y, fmaf(-ri3, D.y, qy[u])));
-            qz[u] = fmaf(cR, rz, fmaf(-cE, E.z, fmaf(-ri3, D.z, qz[u])));
-            if (LJ && inside) {  // tabulated mean LJ force (:291-305)
-                const float dist = __fsqrt_rn(d2);
-                const int bin = (int)__fmaf_rn(__fsub_rn(dist, f_r0), f_inv, 0.5f);
-                if (bin >= 0 && bin < nf) {
-                    const float2 tv = __ldg(a.ftab + frow[u] + bin);
-                    const float fr = (dist - fmaf((float)bin, f_dr, f_r0)) * f_inv;
-                    const float fv = fmaf(fr, tv.y - tv.x, tv.x) * R[0].w * ri;
-                    lx[u] = fmaf(fv, rx, lx[u]);
-                    ly[u] = fmaf(fv, ry, ly[u]);
-                    lz[u] = fmaf(fv, rz, lz[u]);
-                }
-            }
+            point_force<LJ, decltype(far)::value>(s_p[k].q, rx, ry, rz, d2, rm2[u], frow[u], a, qx[u], qy[u], qz[u],
+                                                  lx[u], ly[u], lz[u]);
         };
         int k = 0;
         if (VOTE) {
@@ -588,6 +613,68 @@ __global__ void __launch_bounds__(ForceShape<A>::kThreads, VOTE ? 8 : ForceShape
     pdl_wait();
     pdl_trigger();
     force_item<LJ, A, VOTE>(a, blockIdx.x);
+}
+
+// Forces of a field tile's own np points (records in shared memory) on every
+// atom of its window.  Threads take (atom, point group) pairs: G groups of
+// consecutive points, G = min(np, threads / atoms) (at least 1), so small
+// windows keep the block's threads busy; each pair runs the force pass's
+// per-pair arithmetic, sums its group in FP32 and adds one set of fixed-point
+// atomics per atom and group.
+template <bool LJ>
+__device__ __forceinline__ void tile_point_forces(const ForceArgs &a, const WinDev &W, const PointRec *s_rec,
+                                                  int np) {
+    const float L = W.box, h = W.hbox;
+    const int n = W.n_atoms;
+    const int G = max(1, min(np, (int)blockDim.x / max(n, 1)));
+    const int per = (np + G - 1) / G;
+    for (int idx = threadIdx.x; idx < n * G; idx += blockDim.x) {
+        const int i = idx % n, grp = idx / n;
+        const int k0 = grp * per, k1 = min(np, k0 + per);
+        const int ai = W.atom_off + i;
+        const float4 xi = a.pos[ai];
+        const int ity = a.atype[ai].y;
+        const float rm = __ldg(a.rmax + ity);
+        const float rm2 = __fmul_rn(rm, rm);
+        const int frow = ity * a.n_f;
+        const float vt = __ldg(a.vtot + ity);
+        float qx = 0.f, qy = 0.f, qz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
+#pragma unroll 4
+        for (int k = k0; k < k1; ++k) {
+            const float4 P = s_rec[k].q[0];
+            const float rx = mimg(P.x - xi.x, L, h);
+            const float ry = mimg(P.y - xi.y, L, h);
+            const float rz = mimg(P.z - xi.z, L, h);
+            point_force<LJ, false>(s_rec[k].q, rx, ry, rz, dist2f(rx, ry, rz), rm2, frow, a, qx, qy, qz, lx, ly, lz);
+        }
+        if (k1 <= k0) continue;
+        const float Fx = -vt * fmaf(xi.w, qx, lx);
+        const float Fy = -vt * fmaf(xi.w, qy, ly);
+        const float Fz = -vt * fmaf(xi.w, qz, lz);
+        check_force(a.status, Fx, Fy, Fz);
+        unsigned long long *acc = a.facc + 3 * (long long)ai;
+        atomicAdd(acc + 0, (unsigned long long)to_fix(Fx));
+        atomicAdd(acc + 1, (unsigned long long)to_fix(Fy));
+        atomicAdd(acc + 2, (unsigned long long)to_fix(Fz));
+    }
+}
+
+// Field and force passes fused for small windows: each block computes its
+// tile's points (the field kernel's code, records also kept in shared
+// memory), then those points' forces on every atom of the window.  A point's
+// force on an atom needs only that point's record, so no other block's result
+// is waited for; one launch per step instead of two, and no record round trip
+// through L2.  Forces equal the separate passes' up to FP32 summation order
+// (sums over a tile's points instead of a force work item's).
+template <int S, bool VOTE>
+__global__ void __launch_bounds__(FieldShape<S>::kThreads) field_force_kernel(FieldArgs f, ForceArgs g) {
+    pdl_wait();
+    pdl_trigger();
+    __shared__ PointRec s_rec[FieldShape<S>::kThreads / S];
+    field_tile<S, true, false, VOTE, false, true>(f, blockIdx.x, s_rec);
+    __syncthreads();
+    const int4 tile = f.tiles[blockIdx.x];
+    tile_point_forces<true>(g, f.win[tile.x], s_rec, tile.z);
 }
 
 // The whole MD step in one cooperative launch, for engines whose step is
@@ -713,6 +800,27 @@ cudaError_t launch_step(const StepArgs &a, int grid, cudaStream_t s) {
     cfg.numAttrs = 1;
     if (a.nonbond.terms == 7) return cudaLaunchKernelEx(&cfg, step_kernel<true>, a);
     return cudaLaunchKernelEx(&cfg, step_kernel<false>, a);
+}
+
+bool field_force_fusable(int split) { return split == 4 || split == 8 || split == 16; }
+
+void launch_field_force(const FieldArgs &f, const ForceArgs &g, int split, cudaStream_t s) {
+    if (f.n_tiles <= 0) return;
+    const bool v = f.vote != 0;
+    switch (split) {
+        case 16:
+            if (v) launch_chain(field_force_kernel<16, true>, f.n_tiles, FieldShape<16>::kThreads, s, f, g);
+            else launch_chain(field_force_kernel<16, false>, f.n_tiles, FieldShape<16>::kThreads, s, f, g);
+            break;
+        case 8:
+            if (v) launch_chain(field_force_kernel<8, true>, f.n_tiles, FieldShape<8>::kThreads, s, f, g);
+            else launch_chain(field_force_kernel<8, false>, f.n_tiles, FieldShape<8>::kThreads, s, f, g);
+            break;
+        default:
+            if (v) launch_chain(field_force_kernel<4, true>, f.n_tiles, FieldShape<4>::kThreads, s, f, g);
+            else launch_chain(field_force_kernel<4, false>, f.n_tiles, FieldShape<4>::kThreads, s, f, g);
+            break;
+    }
 }
 
 void launch_force(const ForceArgs &a, cudaStream_t s) {

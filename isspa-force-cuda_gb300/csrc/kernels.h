@@ -284,6 +284,11 @@ inline void launch_chain(void (*k)(P...), unsigned grid, unsigned block, cudaStr
 void launch_adjoint(const AdjointArgs &a, cudaStream_t s);
 void launch_field(const FieldArgs &a, int split, bool raw, cudaStream_t s);
 void launch_force(const ForceArgs &a, cudaStream_t s);
+// Field and force passes as one launch over the field tiles (split 4, 8 or
+// 16, Philox points, tabulated LJ term on): each tile's points act on every
+// atom of its window right after their fields are known.
+bool field_force_fusable(int split);
+void launch_field_force(const FieldArgs &f, const ForceArgs &g, int split, cudaStream_t s);
 void launch_nonbond(const NonbondArgs &a, cudaStream_t s);
 // Cutoff mode: displacement check and (when it trips) the list rebuild; then the pairs.
 void launch_nblist_build(const NbListArgs &a, cudaStream_t s);

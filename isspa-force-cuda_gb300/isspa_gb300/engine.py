@@ -26,7 +26,8 @@ class Engine:
                  force_chunk: int = 0, mem_cap: int = 0, force_atoms_per_thread: int = 0,
                  force_tail_chunk: int = 0, field_vote: int = 0, force_vote: int = 0, integrator: int = 0,
                  nonbond_chunk: int = 0, field_tma: int = 0, nonbond_cutoff: float = 0.0,
-                 nonbond_skin: float = 0.0, nonbond_list_max: int = 0, step_pdl: int = 0):
+                 nonbond_skin: float = 0.0, nonbond_list_max: int = 0, step_pdl: int = 0,
+                 isspa_fused: int = 0):
         if isinstance(windows, System):
             windows = [windows]
         self.windows = list(windows)
@@ -53,6 +54,7 @@ class Engine:
         opt.nonbond_skin = float(nonbond_skin)
         opt.nonbond_list_max = int(nonbond_list_max)
         opt.step_pdl = int(step_pdl)
+        opt.isspa_fused = int(isspa_fused)
         h = C.c_void_p()
         abi.check(L.isspa_engine_create(descs, len(self.windows), C.byref(opt), C.byref(h)), "engine create")
         self._h = h
@@ -67,7 +69,7 @@ class Engine:
         keys = ("field_split", "field_tiles", "force_chunk", "force_items", "nonbond_items",
                 "nonbond_partners_per_item", "sms", "force_atoms_per_thread", "force_tail_chunk",
                 "field_vote", "force_vote", "integrator", "field_tma", "nonbond_list_rows", "nonbond_list_cells",
-                "step_pdl")
+                "step_pdl", "isspa_fused")
         return dict(zip(keys, list(v)))
 
     def nonbond_list_stats(self) -> dict:
