@@ -9,8 +9,9 @@ item's).
 
 * IS-SPA forces of every term mask that keeps the tabulated LJ term, against
   the FP64 oracle (tests/parity.py measures), at field splits 4, 8 and 16,
-  with and without the voted atom loop: ADI2 at nMC 100, a 264-atom window,
-  and three uneven batched windows.
+  with and without the voted atom loop: ADI2 at nMC 100 and a 264-atom
+  window; three uneven batched windows against the separate passes (IS-SPA
+  term) and the oracle (total force).
 * The full step's forces against the oracle, and trajectories against the
   separate passes' (FP32 summation order only: within 1e-5 A after 12 steps).
 * Determinism: graph replays, direct stream launches, programmatic launches
@@ -24,7 +25,7 @@ import pytest
 
 import isspa_gb300 as ig
 import oracle as O
-from parity import check_force
+from parity import check_force, nrel
 
 pytestmark = pytest.mark.gpu
 
@@ -72,14 +73,29 @@ def test_fused_splits_and_votes_match_oracle(split, vote, medium):
 
 
 def test_fused_batched_windows_match_oracle():
+    # The IS-SPA term alone of the 1078-atom window differs from the oracle by
+    # 4.9e-5 per atom in the separate passes too (7e-6 normwise); the total
+    # force, the quantity the step uses, is compared with the oracle as in
+    # test_gpu_parity.py, and the IS-SPA term with the separate passes.
     wins = ig.synth.config_batched(n_windows=3, seed=9)
     f = _fused_isspa(wins, field_split=8)
+    sep = ig.Engine(wins, isspa_fused=2, field_split=8)
+    sep.zero_forces()
+    sep.isspa_force()
+    f_sep = sep.forces()
+    sep.close()
+    fused = ig.Engine(wins, isspa_fused=1, field_split=8)
+    tot = fused.compute_forces()
+    fused.close()
     off = 0
     for k, s in enumerate(wins):
-        o = O.Oracle(s)
-        ref = o.isspa_force(o.mc_points(seed=s.seed, step=0, window=k))
-        check_force(f[off:off + s.n_atoms], ref, f"fused batched window {k} ({s.n_atoms} atoms)")
-        off += s.n_atoms
+        n = s.n_atoms
+        d = nrel(f[off:off + n], f_sep[off:off + n])
+        print(f"fused against separate passes, window {k} ({n} atoms): normwise {d:.2e}")
+        assert d < 1e-6
+        ref, _, _ = O.Oracle(s).total_force(seed=s.seed, step=0, window=k)
+        check_force(tot[off:off + n], ref, f"fused batched window {k} ({n} atoms), total force")
+        off += n
 
 
 def test_fused_full_step_forces_and_trajectory():
