@@ -164,7 +164,7 @@ typedef struct isspa_engine_options {
                               Philox points, the tabulated LJ term and a field split of 4, 8 or
                               16, else the separate passes run).  Forces equal the separate
                               passes' up to FP32 summation order.  2: separate passes; 0 => 2
-                              until isspa_autotune times both (windows of up to 1024 atoms)
+                              until isspa_autotune times both (windows of up to 512 atoms)
                               and keeps the faster */
 } isspa_engine_options;
 

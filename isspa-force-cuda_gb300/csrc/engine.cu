@@ -598,9 +598,9 @@ struct isspa_engine {
 
     // The fused field + force launch needs Philox points, the tabulated LJ term
     // and a field split of 4, 8 or 16; it is offered for windows of at most
-    // kFusedMaxAtoms atoms (its force phase adds one set of atomics per atom
-    // and field tile).
-    static constexpr int kFusedMaxAtoms = 1024;
+    // kFusedMaxAtoms atoms by the autotuner (its force phase adds one set of
+    // atomics per atom and field tile).
+    static constexpr int kFusedMaxAtoms = 512;
     int max_window_atoms() const {
         int m = 0;
         for (const WinDev &d : win_h) m = std::max(m, d.n_atoms);

@@ -619,11 +619,16 @@ __global__ void __launch_bounds__(ForceShape<A>::kThreads, VOTE ? 8 : ForceShape
 // atom of its window.  Threads take (atom, point group) pairs: G groups of
 // consecutive points, G = min(np, threads / atoms) (at least 1), so small
 // windows keep the block's threads busy; each pair runs the force pass's
-// per-pair arithmetic, sums its group in FP32 and adds one set of fixed-point
-// atomics per atom and group.
+// per-pair arithmetic and sums its group in FP32.  The groups' fixed-point
+// values meet in shared memory (s_acc, windows of up to kFusedSmemAtoms
+// atoms), so the block adds one set of global atomics per atom: every block
+// of a small window adds into the same few hundred words, and per-group
+// global atomics queued on them.
+constexpr int kFusedSmemAtoms = 512;
 template <bool LJ>
 __device__ __forceinline__ void tile_point_forces(const ForceArgs &a, const WinDev &W, const PointRec *s_rec,
-                                                  int np) {
+                                                  int np, unsigned long long *s_acc) {
+    const bool smem = W.n_atoms <= kFusedSmemAtoms;
     const float L = W.box, h = W.hbox;
     const int n = W.n_atoms;
     const int G = max(1, min(np, (int)blockDim.x / max(n, 1)));
@@ -652,11 +657,14 @@ __device__ __forceinline__ void tile_point_forces(const ForceArgs &a, const WinD
         const float Fy = -vt * fmaf(xi.w, qy, ly);
         const float Fz = -vt * fmaf(xi.w, qz, lz);
         check_force(a.status, Fx, Fy, Fz);
-        unsigned long long *acc = a.facc + 3 * (long long)ai;
+        unsigned long long *acc = smem ? s_acc + 3 * i : a.facc + 3 * (long long)ai;
         atomicAdd(acc + 0, (unsigned long long)to_fix(Fx));
         atomicAdd(acc + 1, (unsigned long long)to_fix(Fy));
         atomicAdd(acc + 2, (unsigned long long)to_fix(Fz));
     }
+    if (!smem) return;
+    __syncthreads();
+    for (int c = threadIdx.x; c < 3 * n; c += blockDim.x) atomicAdd(a.facc + 3 * (long long)W.atom_off + c, s_acc[c]);
 }
 
 // Field and force passes fused for small windows: each block computes its
@@ -671,10 +679,12 @@ __global__ void __launch_bounds__(FieldShape<S>::kThreads) field_force_kernel(Fi
     pdl_wait();
     pdl_trigger();
     __shared__ PointRec s_rec[FieldShape<S>::kThreads / S];
-    field_tile<S, true, false, VOTE, false, true>(f, blockIdx.x, s_rec);
+    __shared__ unsigned long long s_acc[3 * kFusedSmemAtoms];
+    for (int c = threadIdx.x; c < 3 * kFusedSmemAtoms; c += blockDim.x) s_acc[c] = 0ull;
+    field_tile<S, true, false, VOTE, false, true>(f, blockIdx.x, s_rec);  // (its first barrier orders s_acc)
     __syncthreads();
     const int4 tile = f.tiles[blockIdx.x];
-    tile_point_forces<true>(g, f.win[tile.x], s_rec, tile.z);
+    tile_point_forces<true>(g, f.win[tile.x], s_rec, tile.z, s_acc);
 }
 
 // The whole MD step in one cooperative launch, for engines whose step is
