@@ -606,9 +606,8 @@ struct isspa_engine {
         for (const WinDev &d : win_h) m = std::max(m, d.n_atoms);
         return m;
     }
-    bool fused_ok() const {
-        return !inject && (opt.isspa_terms & 2) && field_force_fusable(field_split) && n_field_tiles > 0;
-    }
+    bool fused_applies() const { return !inject && (opt.isspa_terms & 2) && n_field_tiles > 0; }
+    bool fused_ok() const { return fused_applies() && field_force_fusable(field_split); }
     bool fused() const { return isspa_fused == 1 && fused_ok(); }
 
     // ---------------------------------------------------------- sequences
@@ -1671,7 +1670,8 @@ int isspa_autotune(isspa_engine *e, int reps, int shape[ISSPA_SHAPE_COUNT]) {
         // timed as single-step graph replays; positions, velocities and the
         // step counter are restored afterwards
         ck(cudaMemsetAsync(e->facc, 0, 3 * sizeof(unsigned long long) * e->n_atoms, e->stream));
-        const bool try_fused = e->opt.isspa_fused == 0 && e->fused_ok() && e->max_window_atoms() <= isspa_engine::kFusedMaxAtoms;
+        const bool try_fused = e->opt.isspa_fused == 0 && e->fused_applies() &&
+                               e->max_window_atoms() <= isspa_engine::kFusedMaxAtoms;
         if ((e->opt.integrator == 0 || e->opt.step_pdl == 0 || try_fused) && e->n_atoms > 0) {
             std::vector<float4> p0(e->n_atoms), v0(e->n_atoms);
             uint32_t st0 = 0;
@@ -1681,14 +1681,16 @@ int isspa_autotune(isspa_engine *e, int reps, int shape[ISSPA_SHAPE_COUNT]) {
             ck(cudaStreamSynchronize(e->stream));
             // candidates: the integrators (1, 2, 3) the options leave open, each
             // with and without programmatic launches of the step chain and, for
-            // small windows, with the fused field + force launch (neither in the
-            // single-kernel step); three interleaved rounds, the minimum per
-            // candidate: they differ by a few per cent where they differ
+            // small windows, with the fused field + force launch at field splits
+            // 4, 8 and 16 (its best split need not be the field pass's; neither
+            // in the single-kernel step); three interleaved rounds, the minimum
+            // per candidate: they differ by a few per cent where they differ
             struct Cand {
-                int m, pdl, fused;
+                int m, pdl, fused, split;  // split 0: the field pass's tuned split
             };
             std::vector<Cand> cand;
             const int fixed_fused = e->isspa_fused;
+            const int S0 = e->field_split;
             for (int m : {1, 2, 3}) {
                 if (e->opt.integrator != 0 && m != e->integrator) continue;
                 if (m == 3 && !e->step_kernel_ok()) continue;
@@ -1697,16 +1699,30 @@ int isspa_autotune(isspa_engine *e, int reps, int shape[ISSPA_SHAPE_COUNT]) {
                         if (m == 3 && (pdl || fu)) continue;
                         if (e->opt.step_pdl != 0 && m != 3 && pdl != (e->opt.step_pdl == 1 ? 1 : 0)) continue;
                         if (m != 3 && (try_fused ? false : fu != fixed_fused)) continue;
-                        cand.push_back({m, pdl, fu});
+                        if (fu && e->fused_applies()) {
+                            for (int S : {4, 8, 16})
+                                if (field_force_fusable(S) && (e->opt.field_split == 0 || S == S0))
+                                    cand.push_back({m, pdl, 1, S});
+                        } else {
+                            cand.push_back({m, pdl, fu, 0});
+                        }
                     }
             }
+            // the field split first (leaving the single-kernel step restores the
+            // split it replaced), then the integrator
+            auto apply = [&](const Cand &c) {
+                e->set_integrator(1);
+                const int S = c.split ? c.split : S0;
+                if (e->field_split != S) e->set_field_split(S);
+                e->set_integrator(c.m);
+                e->step_pdl = c.pdl;
+                e->isspa_fused = c.fused;
+            };
             std::vector<float> t(cand.size(), 1e30f);
             int rounds = 3;
             for (int round = 0; round < rounds; ++round)
                 for (size_t c = 0; c < cand.size(); ++c) {
-                    e->set_integrator(cand[c].m);
-                    e->step_pdl = cand[c].pdl;
-                    e->isspa_fused = cand[c].fused;
+                    apply(cand[c]);
                     e->invalidate_graphs();
                     cudaGraphExec_t g = e->capture(1);
                     auto one = [&] { ck(cudaGraphLaunch(g, e->stream)); };
@@ -1721,9 +1737,7 @@ int isspa_autotune(isspa_engine *e, int reps, int shape[ISSPA_SHAPE_COUNT]) {
             size_t best = 0;
             for (size_t c = 1; c < cand.size(); ++c)
                 if (t[c] < t[best]) best = c;
-            e->set_integrator(cand[best].m);
-            e->step_pdl = cand[best].pdl;
-            e->isspa_fused = cand[best].fused;
+            apply(cand[best]);
             ck(cudaMemcpyAsync(e->pos, p0.data(), sizeof(float4) * e->n_atoms, cudaMemcpyHostToDevice, e->stream));
             ck(cudaMemcpyAsync(e->vel, v0.data(), sizeof(float4) * e->n_atoms, cudaMemcpyHostToDevice, e->stream));
             ck(cudaMemcpyAsync(e->d_step, &st0, sizeof(uint32_t), cudaMemcpyHostToDevice, e->stream));

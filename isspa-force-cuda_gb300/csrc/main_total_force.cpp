@@ -74,8 +74,9 @@ int main(int argc, char **argv) {
     if (cfg.n_steps >= 1000) {  // worth a fraction of a second: time the launch-shape candidates once
         int shape[ISSPA_SHAPE_COUNT];
         if ((rc = isspa_autotune(e, 3, shape))) return fail("autotuning", rc);
-        std::printf("launch shapes: field split %d, force chunk %d points (last items %d), %d atom(s) per force thread\n",
-                    shape[0], shape[2], shape[8], shape[7]);
+        std::printf("launch shapes: field split %d, force chunk %d points (last items %d), %d atom(s) per force thread, "
+                    "step integrator %d, programmatic launches %d, fused field + force %d\n",
+                    shape[0], shape[2], shape[8], shape[7], shape[11], shape[15], shape[16]);
     }
     const int n = d.n_atoms;
     std::vector<float> pos(4 * (size_t)n), vel(4 * (size_t)n), frc(4 * (size_t)n);
