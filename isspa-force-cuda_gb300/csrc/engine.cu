@@ -64,8 +64,9 @@ inline void ck(cudaError_t e) {
 
 struct isspa_engine {
     int device = 0;
-    cudaStream_t stream = nullptr, side = nullptr, side2 = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_join2 = nullptr, ev_a = nullptr, ev_b = nullptr;
+    cudaStream_t stream = nullptr, side = nullptr, side2 = nullptr, side3 = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_join2 = nullptr, ev_join3 = nullptr, ev_a = nullptr,
+                ev_b = nullptr;
     isspa_engine_options opt{};
     int n_windows = 0, n_atoms = 0, n_mc = 0;
     long long n_points = 0;
@@ -337,11 +338,12 @@ struct isspa_engine {
         for (auto ev : tev) cudaEventDestroy(ev);
         for (auto ev : kev)
             if (ev) cudaEventDestroy(ev);
-        for (cudaEvent_t ev : {ev_fork, ev_join, ev_join2, ev_a, ev_b})
+        for (cudaEvent_t ev : {ev_fork, ev_join, ev_join2, ev_join3, ev_a, ev_b})
             if (ev) cudaEventDestroy(ev);
         for (void *p : allocs) cudaFree(p);
         if (side) cudaStreamDestroy(side);
         if (side2) cudaStreamDestroy(side2);
+        if (side3) cudaStreamDestroy(side3);
         if (stream) cudaStreamDestroy(stream);
     }
 
@@ -660,9 +662,14 @@ struct isspa_engine {
             mark(ISSPA_K_STEP, 1, stream);
             return;
         }
+        // the umbrella restraint on a branch of its own: with the IS-SPA pass
+        // fused, bonded -> restraint in series bounded a restrained small
+        // window's step
+        const bool us_branch = integrator == 1 && n_us > 0;
         ck(cudaEventRecord(ev_fork, stream));
         ck(cudaStreamWaitEvent(side, ev_fork, 0));
         ck(cudaStreamWaitEvent(side2, ev_fork, 0));
+        if (us_branch) ck(cudaStreamWaitEvent(side3, ev_fork, 0));
         mark(ISSPA_K_FIELD, 0, stream);
         if (fused()) {  // one launch for both passes; timed as the field kernel
             launch_field_force(field_args(), force_args(), field_split, stream);
@@ -678,9 +685,12 @@ struct isspa_engine {
             mark(ISSPA_K_BONDED, 0, side);
             launch_bonded(bonded_args(1, 1, 1), side);
             mark(ISSPA_K_BONDED, 1, side);
-            mark(ISSPA_K_UMBRELLA, 0, side);
-            launch_umbrella(umbrella_args(), side);
-            mark(ISSPA_K_UMBRELLA, 1, side);
+        }
+        if (us_branch) {
+            mark(ISSPA_K_UMBRELLA, 0, side3);
+            launch_umbrella(umbrella_args(), side3);
+            mark(ISSPA_K_UMBRELLA, 1, side3);
+            ck(cudaEventRecord(ev_join3, side3));
         }
         // nonbond on a third branch: for small systems bonded + restraint and
         // nonbond are each as long as the IS-SPA pass, and in series they
@@ -692,6 +702,7 @@ struct isspa_engine {
         ck(cudaEventRecord(ev_join2, side2));
         ck(cudaStreamWaitEvent(stream, ev_join, 0));
         ck(cudaStreamWaitEvent(stream, ev_join2, 0));
+        if (us_branch) ck(cudaStreamWaitEvent(stream, ev_join3, 0));
         if (integrator == 2) {
             mark(ISSPA_K_INTEGRATOR, 0, stream);
             if (n_atoms > 0) ck(launch_integrator(integrator_args(), integ_grid, stream));
@@ -1277,7 +1288,8 @@ int isspa_engine_create(const isspa_system_desc *windows, int n_windows, const i
         ck(cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high));
         ck(cudaStreamCreateWithPriority(&e->side, cudaStreamNonBlocking, prio_high));
         ck(cudaStreamCreateWithPriority(&e->side2, cudaStreamNonBlocking, prio_high));
-        for (cudaEvent_t *ev : {&e->ev_fork, &e->ev_join, &e->ev_join2})
+        ck(cudaStreamCreateWithPriority(&e->side3, cudaStreamNonBlocking, prio_high));
+        for (cudaEvent_t *ev : {&e->ev_fork, &e->ev_join, &e->ev_join2, &e->ev_join3})
             ck(cudaEventCreateWithFlags(ev, cudaEventDisableTiming));
         ck(cudaEventCreate(&e->ev_a));
         ck(cudaEventCreate(&e->ev_b));
