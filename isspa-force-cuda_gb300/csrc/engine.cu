@@ -643,9 +643,9 @@ struct isspa_engine {
         }
         return false;
     }
-    // Step with three independent chains (field -> force; bonded -> umbrella;
-    // nonbond) on forked streams, all adding into the same accumulator, joined
-    // before the update.  With `timed`, CUDA events bracket every kernel on
+    // Step with independent chains (field -> force or the fused launch;
+    // bonded; umbrella; nonbond) on forked streams, all adding into the same
+    // accumulator, joined before the update.  With `timed`, CUDA events bracket every kernel on
     // the stream it runs on.
     void enqueue_step_forked(bool timed = false) {
         // External event-record nodes: a plain cudaEventRecord under capture only
