@@ -1711,13 +1711,15 @@ int isspa_autotune(isspa_engine *e, int reps, int shape[ISSPA_SHAPE_COUNT]) {
                         if (m == 3 && (pdl || fu)) continue;
                         if (e->opt.step_pdl != 0 && m != 3 && pdl != (e->opt.step_pdl == 1 ? 1 : 0)) continue;
                         if (m != 3 && (try_fused ? false : fu != fixed_fused)) continue;
-                        if (fu && e->fused_applies()) {
+                        size_t added = 0;
+                        if (fu && e->fused_applies())
                             for (int S : {4, 8, 16})
-                                if (field_force_fusable(S) && (e->opt.field_split == 0 || S == S0))
+                                if (field_force_fusable(S) && (e->opt.field_split == 0 || S == S0)) {
                                     cand.push_back({m, pdl, 1, S});
-                        } else {
-                            cand.push_back({m, pdl, fu, 0});
-                        }
+                                    ++added;
+                                }
+                        // (a fused choice with no fusable split runs the separate passes)
+                        if (!added) cand.push_back({m, pdl, fu, 0});
                     }
             }
             // the field split first (leaving the single-kernel step restores the

@@ -159,6 +159,13 @@ def test_fused_falls_back_where_it_does_not_apply(medium):
     eng.isspa_force()
     check_force(eng.forces(), o.isspa_force(pts), "injected points with isspa_fused set")
     eng.close()
+    # asked for with a fixed split it cannot take: the autotuner keeps the separate passes
+    eng = ig.Engine(medium, isspa_fused=1, field_split=2)
+    sh = eng.autotune()
+    assert sh["isspa_fused"] == 0 and sh["field_split"] == 2
+    eng.step(3)
+    assert eng.device_status() == 0
+    eng.close()
     for bad in (-1, 3):
         with pytest.raises(RuntimeError):
             ig.Engine(medium, isspa_fused=bad)
