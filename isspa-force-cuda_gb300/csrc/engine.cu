@@ -1714,7 +1714,7 @@ int isspa_autotune(isspa_engine *e, int reps, int shape[ISSPA_SHAPE_COUNT]) {
                         size_t added = 0;
                         if (fu && e->fused_applies())
                             for (int S : {4, 8, 16})
-                                if (field_force_fusable(S) && (e->opt.field_split == 0 || S == S0)) {
+                                if (field_force_fusable(S)) {
                                     cand.push_back({m, pdl, 1, S});
                                     ++added;
                                 }

@@ -159,10 +159,11 @@ def test_fused_falls_back_where_it_does_not_apply(medium):
     eng.isspa_force()
     check_force(eng.forces(), o.isspa_force(pts), "injected points with isspa_fused set")
     eng.close()
-    # asked for with a fixed split it cannot take: the autotuner keeps the separate passes
-    eng = ig.Engine(medium, isspa_fused=1, field_split=2)
+    # asked for where it cannot apply (tabulated LJ term off): the autotuner
+    # times the separate passes only
+    eng = ig.Engine(medium, isspa_fused=1, isspa_terms=5)
     sh = eng.autotune()
-    assert sh["isspa_fused"] == 0 and sh["field_split"] == 2
+    assert sh["isspa_fused"] == 0
     eng.step(3)
     assert eng.device_status() == 0
     eng.close()
