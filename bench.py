@@ -633,12 +633,14 @@ def run_variants(args):
         # chain as programmatic dependents (the pair timed twice, interleaved)
         # isspa_fused 1: field and force passes as one launch (field split 4, 8
         # or 16 only; the engine reports 0 where it falls back)
-        runs = [("mode1", 1, 0, 2, 2), ("mode1_pdl", 1, 0, 1, 2), ("mode1_pdl_fused", 1, 0, 1, 1),
-                ("mode2", 2, 0, 2, 2), ("mode2_pdl", 2, 0, 1, 2), ("mode3", 3, 0, 2, 2),
-                ("mode1_field_tma", 1, 1, 2, 2), ("mode1_again", 1, 0, 2, 2), ("mode1_pdl_again", 1, 0, 1, 2),
-                ("mode1_pdl_fused_again", 1, 0, 1, 1)]
-        for label, mode, tma, pdl, fused in runs:
-            o = dict(base, integrator=mode, field_tma=tma, step_pdl=pdl, isspa_fused=fused)
+        # force_overlap 1: force items start on stamped field tiles
+        runs = [("mode1", 1, 0, 2, 2, 2), ("mode1_pdl", 1, 0, 1, 2, 2), ("mode1_pdl_overlap", 1, 0, 1, 2, 1),
+                ("mode1_pdl_fused", 1, 0, 1, 1, 2), ("mode2", 2, 0, 2, 2, 2), ("mode2_pdl", 2, 0, 1, 2, 2),
+                ("mode3", 3, 0, 2, 2, 2), ("mode1_field_tma", 1, 1, 2, 2, 2), ("mode1_again", 1, 0, 2, 2, 2),
+                ("mode1_pdl_again", 1, 0, 1, 2, 2), ("mode1_pdl_overlap_again", 1, 0, 1, 2, 1),
+                ("mode1_pdl_fused_again", 1, 0, 1, 1, 2)]
+        for label, mode, tma, pdl, fused, ov in runs:
+            o = dict(base, integrator=mode, field_tma=tma, step_pdl=pdl, isspa_fused=fused, force_overlap=ov)
             if mode == 3:
                 o.update(field_split=4, field_vote=0, force_vote=0)
             e = ig.Engine(system, **o)
@@ -653,6 +655,7 @@ def run_variants(args):
             _, kern = e.time_steps_detailed(min(steps, 50), L2_FLUSH)
             res[label] = {"integrator": e.shapes()["integrator"], "field_tma": e.shapes()["field_tma"],
                           "step_pdl": e.shapes()["step_pdl"], "isspa_fused": e.shapes()["isspa_fused"],
+                          "force_overlap": e.shapes()["force_overlap"],
                           "step_ms": round(ms, 5), "run_ms_per_step": round(run_ms, 5),
                           "kernel_ms": {k: round(v[0] / v[1], 5) for k, v in kern.items() if v[1]},
                           "device_status": e.device_status()}
@@ -704,7 +707,8 @@ def run_profile_case(args):
                         force_vote=fixed["force_vote"], integrator=fixed["integrator"],
                         nonbond_chunk=fixed["nonbond_partners_per_item"], field_tma=fixed["field_tma"],
                         step_pdl=1 if fixed.setdefault("step_pdl", 0) else 2,
-                        isspa_fused=1 if fixed.setdefault("isspa_fused", 0) else 2)
+                        isspa_fused=1 if fixed.setdefault("isspa_fused", 0) else 2,
+                        force_overlap=1 if fixed.setdefault("force_overlap", 0) else 2)
         shapes = eng.shapes()
         if shapes != fixed:
             raise RuntimeError(f"shapes from {args.shapes_file} not reproduced: {shapes} != {fixed}")

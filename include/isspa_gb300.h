@@ -166,6 +166,14 @@ typedef struct isspa_engine_options {
                               passes' up to FP32 summation order.  2: separate passes; 0 => 2
                               until isspa_autotune times both (windows of up to 512 atoms)
                               and keeps the faster */
+    int force_overlap;     /* 1: in isspa_step the field blocks stamp their tiles when their
+                              point records are written, and each force work item waits
+                              (bounded; ISSPA_ERR_TIMEOUT from isspa_device_status if it gives
+                              up) only for the tiles its points lie in, so with programmatic
+                              launches the force pass starts in the field pass's last wave
+                              (same results bit for bit; not with the fused launch or the
+                              single-kernel step).  2: the force pass waits for the whole field
+                              pass; 0 => 2 until isspa_autotune times both and keeps the faster */
 } isspa_engine_options;
 
 #define ISSPA_TERMS_NONE (-1)
@@ -234,8 +242,9 @@ int isspa_engine_info(const isspa_engine *e, int *n_windows, int *n_atoms_total,
  * cutoff mode the partners a neighbour-list row holds (0 otherwise), [14] in
  * cutoff mode the cells of all windows' cell grids (0 otherwise), [15] 1 when
  * isspa_step launches its kernel chain as programmatic dependents, [16] 1 when
- * the field and force passes run as one fused launch. */
-#define ISSPA_SHAPE_COUNT 17
+ * the field and force passes run as one fused launch, [17] 1 when the step's
+ * force items start on stamped field tiles (force_overlap). */
+#define ISSPA_SHAPE_COUNT 18
 int isspa_engine_shapes(const isspa_engine *e, int shape[ISSPA_SHAPE_COUNT]);
 /* Autotuner: times every field-pass atom split (per-pair and warp-voted
  * loops, atoms staged by loads or by bulk copies) and, for 1 and 2 receiving
@@ -245,10 +254,11 @@ int isspa_engine_shapes(const isspa_engine *e, int shape[ISSPA_SHAPE_COUNT]);
  * chosen list) on this engine's own
  * workload with CUDA events (reps launches each), keeps the fastest of each
  * and reports the result as isspa_engine_shapes does.  When the options leave
- * the integrator, step_pdl or isspa_fused open (0), it then times single-step
- * graph replays of the open choices (separate kernels, fused integrator,
- * single-kernel step; with and without programmatic launches; with and
- * without the fused field + force launch) and keeps the fastest (the nonbond
+ * the integrator, step_pdl, isspa_fused or force_overlap open (0), it then
+ * times single-step graph replays of the open choices (separate kernels, fused
+ * integrator, single-kernel step; with and without programmatic launches;
+ * the fused field + force launch or the separate passes, with and without
+ * force_overlap) and keeps the fastest (the nonbond
  * partners per item are timed too); positions,
  * velocities and the step counter are restored.  Clears the force
  * accumulator; invalidates captured graphs. */

@@ -94,6 +94,11 @@ struct isspa_engine {
     int field_tma = 0;   // field pass stages its atom rounds by 1-D bulk copies (TMA)
     int step_pdl = 0;    // step chain launched as programmatic dependents (1) or not (0)
     int isspa_fused = 0;  // field and force passes as one launch (1) when fused_ok()
+    int force_overlap = 0;  // force items start on stamped field tiles (1) when overlap_ok()
+    unsigned int *tile_flag = nullptr;  // per field tile: the stamp of the pass that wrote its records
+    size_t tile_flag_cap = 0;
+    int *tile_base = nullptr;           // per window: its first field tile
+    unsigned int *ov_epoch = nullptr;   // [0] stamp of the current pass - 1, [1] force items done
     int force_vote = 0;  // force pass in warp-voted groups of four points (1 atom per thread)
     int force_apt = 1;  // receiving atoms per force-kernel thread (1 or 2)
     // step integrator: 1 = bonded, umbrella and leapfrog kernels (bonded and
@@ -238,8 +243,10 @@ struct isspa_engine {
     }
     void set_field_split(int S) {
         std::vector<int4> t;
+        std::vector<int> base(win_h.size(), 0);
         const int tp = field_points_per_block(S);
         for (int w : order) {
+            base[w] = (int)t.size();
             const long long P = (long long)win_h[w].n_atoms * n_mc;
             for (long long p = 0; p < P; p += tp)
                 t.push_back(make_int4(w, (int)(win_h[w].point_off + p), (int)std::min<long long>(tp, P - p), 0));
@@ -248,6 +255,14 @@ struct isspa_engine {
         field_tiles = upload(t);
         n_field_tiles = (int)t.size();
         field_split = S;
+        release(tile_base);
+        tile_base = upload(base);
+        if (t.size() > tile_flag_cap) {  // fresh stamps are 0, never a pass's stamp
+            release(tile_flag);
+            tile_flag = alloc<unsigned int>(t.size());
+            ck(cudaMemset(tile_flag, 0, t.size() * sizeof(unsigned int)));
+            tile_flag_cap = t.size();
+        }
     }
     // Force work items: C-point chunks of every window, then (Ct > 0) the last
     // stretch of every window's points in Ct-point chunks, listed after all
@@ -611,6 +626,12 @@ struct isspa_engine {
     bool fused_applies() const { return !inject && (opt.isspa_terms & 2) && n_field_tiles > 0; }
     bool fused_ok() const { return fused_applies() && field_force_fusable(field_split); }
     bool fused() const { return isspa_fused == 1 && fused_ok(); }
+    // Force items starting on stamped field tiles: the step's separate passes
+    // (launched by isspa_step; the per-call functions keep plain launches)
+    bool overlap_ok() const {
+        return integrator != 3 && !fused() && opt.isspa_terms && n_field_tiles > 0 && n_force_items > 0;
+    }
+    bool overlap() const { return force_overlap == 1 && overlap_ok(); }
 
     // ---------------------------------------------------------- sequences
     void enqueue_isspa(cudaStream_t s, bool raw = false) {
@@ -675,10 +696,21 @@ struct isspa_engine {
             launch_field_force(field_args(), force_args(), field_split, stream);
             mark(ISSPA_K_FIELD, 1, stream);
         } else {
-            launch_field(field_args(), field_split, false, stream);
+            FieldArgs fa = field_args();
+            ForceArgs ga = force_args();
+            if (overlap()) {
+                fa.tile_flag = tile_flag;
+                fa.ov_epoch = ov_epoch;
+                ga.overlap = 1;
+                ga.tile_flag = tile_flag;
+                ga.ov_epoch = ov_epoch;
+                ga.tile_base = tile_base;
+                ga.tile_pts = field_points_per_block(field_split);
+            }
+            launch_field(fa, field_split, false, stream);
             mark(ISSPA_K_FIELD, 1, stream);
             mark(ISSPA_K_FORCE, 0, stream);
-            launch_force(force_args(), stream);
+            launch_force(ga, stream);
             mark(ISSPA_K_FORCE, 1, stream);
         }
         if (integrator == 1) {
@@ -1011,6 +1043,7 @@ void build(isspa_engine &E, const std::vector<isspa_host_system> &ws) {
     E.field_tma = E.opt.field_tma == 1 ? 1 : 0;
     E.step_pdl = E.opt.step_pdl == 1 ? 1 : 0;
     E.isspa_fused = E.opt.isspa_fused == 1 ? 1 : 0;
+    E.force_overlap = E.opt.force_overlap == 1 ? 1 : 0;
     E.force_vote = E.opt.force_vote == 1 ? 1 : 0;
     E.force_apt = E.opt.force_atoms_per_thread == 2 ? 2 : 1;
     E.set_force_chunk(E.opt.force_chunk > 0 ? E.opt.force_chunk : E.default_force_chunk(),
@@ -1097,6 +1130,8 @@ void build(isspa_engine &E, const std::vector<isspa_host_system> &ws) {
     E.status = E.alloc<int>(1);
     E.d_step = E.alloc<uint32_t>(1);
     E.d_done = E.alloc<unsigned int>(1);
+    E.ov_epoch = E.alloc<unsigned int>(2);
+    ck(cudaMemset(E.ov_epoch, 0, 2 * sizeof(unsigned int)));
     ck(cudaMemset(E.status, 0, sizeof(int)));
     ck(cudaMemset(E.d_step, 0, sizeof(uint32_t)));
     ck(cudaMemset(E.d_done, 0, sizeof(unsigned int)));
@@ -1273,7 +1308,8 @@ int isspa_engine_create(const isspa_system_desc *windows, int n_windows, const i
     else if (e->opt.nonbond_terms == 0) e->opt.nonbond_terms = 7;
     if (!(e->opt.nonbond_cutoff >= 0.f) || !(e->opt.nonbond_skin >= 0.f) || e->opt.nonbond_list_max < 0 ||
         std::isinf(e->opt.nonbond_cutoff) || std::isinf(e->opt.nonbond_skin) || e->opt.step_pdl < 0 ||
-        e->opt.step_pdl > 2 || e->opt.isspa_fused < 0 || e->opt.isspa_fused > 2)
+        e->opt.step_pdl > 2 || e->opt.isspa_fused < 0 || e->opt.isspa_fused > 2 || e->opt.force_overlap < 0 ||
+        e->opt.force_overlap > 2)
         return ISSPA_ERR_ARG;
     if (cudaGetDevice(&e->device) != cudaSuccess) {
         cudaGetLastError();
@@ -1334,6 +1370,7 @@ int isspa_engine_shapes(const isspa_engine *e, int shape[ISSPA_SHAPE_COUNT]) {
     shape[14] = e->cutoff ? e->nbl_cells : 0;
     shape[15] = e->step_pdl;
     shape[16] = e->fused() ? 1 : 0;
+    shape[17] = e->overlap() ? 1 : 0;
     return ISSPA_OK;
 }
 
@@ -1684,7 +1721,8 @@ int isspa_autotune(isspa_engine *e, int reps, int shape[ISSPA_SHAPE_COUNT]) {
         ck(cudaMemsetAsync(e->facc, 0, 3 * sizeof(unsigned long long) * e->n_atoms, e->stream));
         const bool try_fused = e->opt.isspa_fused == 0 && e->fused_applies() &&
                                e->max_window_atoms() <= isspa_engine::kFusedMaxAtoms;
-        if ((e->opt.integrator == 0 || e->opt.step_pdl == 0 || try_fused) && e->n_atoms > 0) {
+        const bool try_overlap = e->opt.force_overlap == 0 && e->opt.isspa_terms && e->n_force_items > 0;
+        if ((e->opt.integrator == 0 || e->opt.step_pdl == 0 || try_fused || try_overlap) && e->n_atoms > 0) {
             std::vector<float4> p0(e->n_atoms), v0(e->n_atoms);
             uint32_t st0 = 0;
             ck(cudaMemcpyAsync(p0.data(), e->pos, sizeof(float4) * e->n_atoms, cudaMemcpyDeviceToHost, e->stream));
@@ -1692,16 +1730,19 @@ int isspa_autotune(isspa_engine *e, int reps, int shape[ISSPA_SHAPE_COUNT]) {
             ck(cudaMemcpyAsync(&st0, e->d_step, sizeof(uint32_t), cudaMemcpyDeviceToHost, e->stream));
             ck(cudaStreamSynchronize(e->stream));
             // candidates: the integrators (1, 2, 3) the options leave open, each
-            // with and without programmatic launches of the step chain and, for
-            // small windows, with the fused field + force launch at field splits
-            // 4, 8 and 16 (its best split need not be the field pass's; neither
-            // in the single-kernel step); three interleaved rounds, the minimum
-            // per candidate: they differ by a few per cent where they differ
+            // with and without programmatic launches of the step chain; the
+            // separate passes with and without force items starting on stamped
+            // field tiles, and, for small windows, the fused field + force
+            // launch at field splits 4, 8 and 16 (its best split need not be the
+            // field pass's; none of these in the single-kernel step); three
+            // interleaved rounds, the minimum per candidate: they differ by a
+            // few per cent where they differ
             struct Cand {
-                int m, pdl, fused, split;  // split 0: the field pass's tuned split
+                int m, pdl, fused, split, ov;  // split 0: the field pass's tuned split
             };
             std::vector<Cand> cand;
             const int fixed_fused = e->isspa_fused;
+            const int fixed_ov = e->force_overlap;
             const int S0 = e->field_split;
             for (int m : {1, 2, 3}) {
                 if (e->opt.integrator != 0 && m != e->integrator) continue;
@@ -1715,11 +1756,16 @@ int isspa_autotune(isspa_engine *e, int reps, int shape[ISSPA_SHAPE_COUNT]) {
                         if (fu && e->fused_applies())
                             for (int S : {4, 8, 16})
                                 if (field_force_fusable(S)) {
-                                    cand.push_back({m, pdl, 1, S});
+                                    cand.push_back({m, pdl, 1, S, 0});
                                     ++added;
                                 }
-                        // (a fused choice with no fusable split runs the separate passes)
-                        if (!added) cand.push_back({m, pdl, fu, 0});
+                        if (added) continue;
+                        // the separate passes (also a fused choice with no fusable split)
+                        for (int ov : {0, 1}) {
+                            if (m == 3 && ov) continue;
+                            if (m != 3 && (try_overlap ? false : ov != fixed_ov)) continue;
+                            cand.push_back({m, pdl, fu, 0, ov});
+                        }
                     }
             }
             // the field split first (leaving the single-kernel step restores the
@@ -1731,6 +1777,7 @@ int isspa_autotune(isspa_engine *e, int reps, int shape[ISSPA_SHAPE_COUNT]) {
                 e->set_integrator(c.m);
                 e->step_pdl = c.pdl;
                 e->isspa_fused = c.fused;
+                e->force_overlap = c.ov;
             };
             std::vector<float> t(cand.size(), 1e30f);
             int rounds = 3;

@@ -430,11 +430,28 @@ __device__ __forceinline__ void field_tile(const FieldArgs &a, int tile_index, P
     }
 }
 
+__device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int *p) {
+    unsigned int v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned int *p, unsigned int v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
 template <int S, bool GEN, bool RAW, bool VOTE, bool TMA = false>
 __global__ void __launch_bounds__(FieldShape<S>::kThreads) field_kernel(FieldArgs a) {
     pdl_wait();
     pdl_trigger();
     field_tile<S, GEN, RAW, VOTE, TMA>(a, blockIdx.x);
+    if (a.tile_flag) {  // the tile's records are written: stamp it for the force items
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const unsigned int stamp = *a.ov_epoch + 1u;
+            __threadfence();
+            st_release_u32(a.tile_flag + blockIdx.x, stamp);
+        }
+    }
 }
 
 // LJ = include the tabulated mean LJ force (term bit 2); the multipole and CDD
@@ -607,12 +624,63 @@ __device__ __forceinline__ void force_item(const ForceArgs &a, int item_index) {
     }
 }
 
+// Overlap mode: thread 0 waits until every field tile that holds a point of
+// this item's chunk carries the current stamp (the wait gives up after
+// kOverlapWaitNs of global time: kStatusTimeout, and the item adds nothing).
+// Deadlock-free under a programmatic launch, whose blocks are scheduled only
+// once every field block has started; after an ordinary launch the stamps
+// are all in place.
+constexpr unsigned long long kOverlapWaitNs = 500000000ull;
+__device__ __forceinline__ bool wait_item_tiles(const ForceArgs &a, int item_index) {
+    __shared__ int s_ok;
+    if (threadIdx.x == 0) {
+        const int4 item = a.items[item_index];
+        const WinDev W = a.win[item.x];
+        const int2 ch = a.chunks[item.w];
+        const unsigned int stamp = *a.ov_epoch + 1u;
+        const long long q0 = (long long)ch.x - W.point_off, q1 = q0 + ch.y - 1;
+        const int base = a.tile_base[item.x];
+        const int t1 = base + (int)(q1 / a.tile_pts);
+        int ok = 1;
+        const unsigned long long t_start = global_ns();
+        for (int tt = base + (int)(q0 / a.tile_pts); ok && tt <= t1; ++tt)
+            while (ld_acquire_u32(a.tile_flag + tt) != stamp) {
+                if (global_ns() - t_start > kOverlapWaitNs) {
+                    atomicOr(a.status, kStatusTimeout);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(128);
+            }
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+// Overlap mode: the last item to finish advances the stamp for the next pass.
+__device__ __forceinline__ void count_item_done(const ForceArgs &a) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(a.ov_epoch + 1, 1u) == gridDim.x - 1) {
+            a.ov_epoch[1] = 0u;
+            __threadfence();
+            atomicAdd(a.ov_epoch, 1u);
+        }
+    }
+}
+
 template <bool LJ, int A, bool VOTE = false>
 __global__ void __launch_bounds__(ForceShape<A>::kThreads, VOTE ? 8 : ForceShape<A>::kMinBlocks)
     force_kernel(ForceArgs a) {
-    pdl_wait();
+    if (!a.overlap) pdl_wait();
     pdl_trigger();
-    force_item<LJ, A, VOTE>(a, blockIdx.x);
+    if (a.overlap) {
+        if (wait_item_tiles(a, blockIdx.x)) force_item<LJ, A, VOTE>(a, blockIdx.x);
+        count_item_done(a);
+    } else {
+        force_item<LJ, A, VOTE>(a, blockIdx.x);
+    }
 }
 
 // Forces of a field tile's own np points (records in shared memory) on every

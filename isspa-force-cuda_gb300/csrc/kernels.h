@@ -30,6 +30,10 @@ struct FieldArgs {
     int *status;
     int vote;              // 1: atom loop in warp-voted groups of four (same results)
     int tma;               // 1: atom rounds staged by 1-D bulk copies (TMA) behind mbarriers (same results)
+    // overlap with the force pass: each block stamps tile_flag[tile] with
+    // *ov_epoch + 1 once its records are written (nullptr: no stamps)
+    unsigned int *tile_flag;
+    const unsigned int *ov_epoch;
 };
 
 // ---- IS-SPA force pass (one thread per receiving atom) -------------------
@@ -51,6 +55,15 @@ struct ForceArgs {
     int vote;              // 1: points in warp-voted groups of four (same results)
     unsigned long long *facc;  // [Ntot][3]
     int *status;
+    // overlap with the field pass (overlap = 1): instead of waiting for the
+    // whole field kernel, an item waits (bounded) for the stamps of the field
+    // tiles its chunk covers (tile_base[window] + point / tile_pts); the last
+    // item to finish advances ov_epoch[0] (ov_epoch[1]: completion count)
+    int overlap;
+    const unsigned int *tile_flag;
+    unsigned int *ov_epoch;
+    const int *tile_base;
+    int tile_pts;
 };
 
 // ---- all-pairs nonbond --------------------------------------------------

@@ -55,7 +55,7 @@ class EngineOptions(C.Structure):
                 ("field_vote", C.c_int), ("force_vote", C.c_int), ("integrator", C.c_int),
                 ("nonbond_chunk", C.c_int), ("field_tma", C.c_int), ("nonbond_cutoff", C.c_float),
                 ("nonbond_skin", C.c_float), ("nonbond_list_max", C.c_int), ("step_pdl", C.c_int),
-                ("isspa_fused", C.c_int)]
+                ("isspa_fused", C.c_int), ("force_overlap", C.c_int)]
 
 
 class RunConfig(C.Structure):
@@ -82,7 +82,7 @@ class NoallocInputs(C.Structure):
 NOALLOC_SCRATCH_BYTES = 16 << 20
 # ISSPA_NOALLOC_STATUS_* bits written to isspa_noalloc_inputs.status_out
 NOALLOC_STATUS_OVERFLOW, NOALLOC_STATUS_NONFINITE, NOALLOC_STATUS_BOUNDS = 1, 2, 4
-SHAPE_COUNT = 17  # ISSPA_SHAPE_COUNT
+SHAPE_COUNT = 18  # ISSPA_SHAPE_COUNT
 TERMS_NONE = -1  # ISSPA_TERMS_NONE: switches the IS-SPA or nonbond pass off
 
 # isspa_energies components (the ISSPA_E_* enum), kcal/mol

@@ -27,7 +27,7 @@ class Engine:
                  force_tail_chunk: int = 0, field_vote: int = 0, force_vote: int = 0, integrator: int = 0,
                  nonbond_chunk: int = 0, field_tma: int = 0, nonbond_cutoff: float = 0.0,
                  nonbond_skin: float = 0.0, nonbond_list_max: int = 0, step_pdl: int = 0,
-                 isspa_fused: int = 0):
+                 isspa_fused: int = 0, force_overlap: int = 0):
         if isinstance(windows, System):
             windows = [windows]
         self.windows = list(windows)
@@ -55,6 +55,7 @@ class Engine:
         opt.nonbond_list_max = int(nonbond_list_max)
         opt.step_pdl = int(step_pdl)
         opt.isspa_fused = int(isspa_fused)
+        opt.force_overlap = int(force_overlap)
         h = C.c_void_p()
         abi.check(L.isspa_engine_create(descs, len(self.windows), C.byref(opt), C.byref(h)), "engine create")
         self._h = h
@@ -69,7 +70,7 @@ class Engine:
         keys = ("field_split", "field_tiles", "force_chunk", "force_items", "nonbond_items",
                 "nonbond_partners_per_item", "sms", "force_atoms_per_thread", "force_tail_chunk",
                 "field_vote", "force_vote", "integrator", "field_tma", "nonbond_list_rows", "nonbond_list_cells",
-                "step_pdl", "isspa_fused")
+                "step_pdl", "isspa_fused", "force_overlap")
         return dict(zip(keys, list(v)))
 
     def nonbond_list_stats(self) -> dict:
