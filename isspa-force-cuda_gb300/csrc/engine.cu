@@ -98,7 +98,7 @@ struct isspa_engine {
     unsigned int *tile_flag = nullptr;  // per field tile: the stamp of the pass that wrote its records
     size_t tile_flag_cap = 0;
     int *tile_base = nullptr;           // per window: its first field tile
-    unsigned int *ov_epoch = nullptr;   // [0] stamp of the current pass - 1, [1] force items done
+    unsigned int *ov_epoch = nullptr;   // stamp of the current pass - 1 (advanced with the step counter)
     int force_vote = 0;  // force pass in warp-voted groups of four points (1 atom per thread)
     int force_apt = 1;  // receiving atoms per force-kernel thread (1 or 2)
     // step integrator: 1 = bonded, umbrella and leapfrog kernels (bonded and
@@ -549,6 +549,7 @@ struct isspa_engine {
         a.step_ptr = d_step;
         a.done_ptr = d_done;
         a.status = status;
+        a.ov_epoch = ov_epoch;
         return a;
     }
 
@@ -1130,8 +1131,8 @@ void build(isspa_engine &E, const std::vector<isspa_host_system> &ws) {
     E.status = E.alloc<int>(1);
     E.d_step = E.alloc<uint32_t>(1);
     E.d_done = E.alloc<unsigned int>(1);
-    E.ov_epoch = E.alloc<unsigned int>(2);
-    ck(cudaMemset(E.ov_epoch, 0, 2 * sizeof(unsigned int)));
+    E.ov_epoch = E.alloc<unsigned int>(1);
+    ck(cudaMemset(E.ov_epoch, 0, sizeof(unsigned int)));
     ck(cudaMemset(E.status, 0, sizeof(int)));
     ck(cudaMemset(E.d_step, 0, sizeof(uint32_t)));
     ck(cudaMemset(E.d_done, 0, sizeof(unsigned int)));

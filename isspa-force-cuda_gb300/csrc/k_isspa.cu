@@ -657,30 +657,12 @@ __device__ __forceinline__ bool wait_item_tiles(const ForceArgs &a, int item_ind
     __syncthreads();
     return s_ok != 0;
 }
-// Overlap mode: the last item to finish advances the stamp for the next pass.
-__device__ __forceinline__ void count_item_done(const ForceArgs &a) {
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        if (atomicAdd(a.ov_epoch + 1, 1u) == gridDim.x - 1) {
-            a.ov_epoch[1] = 0u;
-            __threadfence();
-            atomicAdd(a.ov_epoch, 1u);
-        }
-    }
-}
-
 template <bool LJ, int A, bool VOTE = false>
 __global__ void __launch_bounds__(ForceShape<A>::kThreads, VOTE ? 8 : ForceShape<A>::kMinBlocks)
     force_kernel(ForceArgs a) {
     if (!a.overlap) pdl_wait();
     pdl_trigger();
-    if (a.overlap) {
-        if (wait_item_tiles(a, blockIdx.x)) force_item<LJ, A, VOTE>(a, blockIdx.x);
-        count_item_done(a);
-    } else {
-        force_item<LJ, A, VOTE>(a, blockIdx.x);
-    }
+    if (!a.overlap || wait_item_tiles(a, blockIdx.x)) force_item<LJ, A, VOTE>(a, blockIdx.x);
 }
 
 // Forces of a field tile's own np points (records in shared memory) on every

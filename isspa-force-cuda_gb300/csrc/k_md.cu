@@ -64,7 +64,10 @@ __global__ void leapfrog_kernel(LeapfrogArgs a) {
     if (i < a.n_atoms) leapfrog_atom(a, i, step, nullptr);
     __syncthreads();
     if (gridDim.x == 1) {
-        if (threadIdx.x == 0) *a.step_ptr = step + 1u;
+        if (threadIdx.x == 0) {
+            *a.step_ptr = step + 1u;
+            if (a.ov_epoch) ++*a.ov_epoch;
+        }
         return;
     }
     if (threadIdx.x == 0) {
@@ -72,6 +75,7 @@ __global__ void leapfrog_kernel(LeapfrogArgs a) {
         const unsigned int prev = atomicAdd(a.done_ptr, 1u);
         if (prev == gridDim.x - 1) {
             *a.step_ptr = step + 1u;
+            if (a.ov_epoch) ++*a.ov_epoch;
             *a.done_ptr = 0u;
             __threadfence();
         }

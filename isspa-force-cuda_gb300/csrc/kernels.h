@@ -57,8 +57,8 @@ struct ForceArgs {
     int *status;
     // overlap with the field pass (overlap = 1): instead of waiting for the
     // whole field kernel, an item waits (bounded) for the stamps of the field
-    // tiles its chunk covers (tile_base[window] + point / tile_pts); the last
-    // item to finish advances ov_epoch[0] (ov_epoch[1]: completion count)
+    // tiles its chunk covers (tile_base[window] + point / tile_pts); the
+    // update kernel advances *ov_epoch with the step counter
     int overlap;
     const unsigned int *tile_flag;
     unsigned int *ov_epoch;
@@ -164,6 +164,7 @@ struct LeapfrogArgs {
     uint32_t *step_ptr;        // advanced by the last block to finish
     unsigned int *done_ptr;    // block-completion counter (self-resetting)
     int *status;
+    unsigned int *ov_epoch;    // advanced with the step counter (the field-tile stamps' base)
 };
 
 // Fused integrator: the bonded terms, the umbrella restraint and leapfrog of a

@@ -557,7 +557,10 @@ __device__ __forceinline__ void integrate_atoms(const IntegratorArgs &a, uint32_
         }
         leapfrog_atom(a.lf, (int)i, step, extra);
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) *a.lf.step_ptr = step + 1u;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        *a.lf.step_ptr = step + 1u;
+        if (a.lf.ov_epoch) ++*a.lf.ov_epoch;
+    }
 }
 
 }  // namespace
