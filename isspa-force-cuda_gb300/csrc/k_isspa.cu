@@ -443,16 +443,14 @@ template <int S, bool GEN, bool RAW, bool VOTE, bool TMA = false>
 __global__ void __launch_bounds__(FieldShape<S>::kThreads) field_kernel(FieldArgs a) {
     pdl_wait();
     pdl_trigger();
-    // the stamp is read before the tile's work (kept in shared memory), so the
-    // block's exit does not wait on it
-    __shared__ unsigned int s_stamp;
-    if (a.tile_flag && threadIdx.x == 0) s_stamp = *a.ov_epoch + 1u;
     field_tile<S, GEN, RAW, VOTE, TMA>(a, blockIdx.x);
-    if (a.tile_flag) {
-        // the tile's records are written: the barrier orders every thread's
-        // stores before thread 0's release, which the force items acquire
+    if (a.tile_flag) {  // the tile's records are written: stamp it for the force items
         __syncthreads();
-        if (threadIdx.x == 0) st_release_u32(a.tile_flag + blockIdx.x, s_stamp);
+        if (threadIdx.x == 0) {
+            const unsigned int stamp = *a.ov_epoch + 1u;
+            __threadfence();
+            st_release_u32(a.tile_flag + blockIdx.x, stamp);
+        }
     }
 }
 
@@ -514,35 +512,9 @@ __device__ __forceinline__ void point_force(const float4 *R, float rx, float ry,
 // takes the out-of-range records without the per-pair select and tabulated-LJ
 // branch.  Same operations in the same order as the per-pair loop.  It keeps
 // four points' geometry live (64 registers, 8 blocks per SM).
-// Overlap mode (a.overlap): thread 0 waits until every field tile that holds
-// a point of the chunk [q0, q1] (window points) carries the stamp; the wait
-// gives up after kOverlapWaitNs of global time (kStatusTimeout, and the item
-// adds nothing).  Deadlock-free under a programmatic launch, whose blocks are
-// scheduled only once every field block has started; after an ordinary
-// launch the stamps are all in place.
-constexpr unsigned long long kOverlapWaitNs = 500000000ull;
-__device__ __forceinline__ bool wait_tiles(const ForceArgs &a, int window, long long q0, long long q1,
-                                           unsigned int stamp) {
-    const int base = a.tile_base[window];
-    const int t1 = base + (int)(q1 / a.tile_pts);
-    const unsigned long long t_start = global_ns();
-    for (int tt = base + (int)(q0 / a.tile_pts); tt <= t1; ++tt)
-        while (ld_acquire_u32(a.tile_flag + tt) != stamp) {
-            if (global_ns() - t_start > kOverlapWaitNs) {
-                atomicOr(a.status, kStatusTimeout);
-                return false;
-            }
-            __nanosleep(128);
-        }
-    return true;
-}
-
 template <bool LJ, int A, bool VOTE = false>
 __device__ __forceinline__ void force_item(const ForceArgs &a, int item_index) {
     static_assert(!VOTE || A == 1, "the voted loop takes one receiving atom per thread");
-    __shared__ int s_go;
-    // (overlap) the stamp, read while the item's own loads are in flight
-    const unsigned int stamp = a.overlap && threadIdx.x == 0 ? *a.ov_epoch + 1u : 0u;
     constexpr int kT = ForceShape<A>::kThreads;
     __shared__ PointRec s_p[kForceThreads];
     const int4 item = a.items[item_index];
@@ -579,11 +551,7 @@ __device__ __forceinline__ void force_item(const ForceArgs &a, int item_index) {
 #pragma unroll
         for (int u = 0; u < A; ++u) qx[u] = qy[u] = qz[u] = lx[u] = ly[u] = lz[u] = 0.f;
         const int pn = min(kForceThreads, ch.y - p0);
-        if (a.overlap && p0 == 0 && t == 0)  // the atoms' loads above overlap the wait
-            s_go = wait_tiles(a, item.x, (long long)ch.x - W.point_off, (long long)ch.x - W.point_off + ch.y - 1,
-                              stamp);
         __syncthreads();
-        if (a.overlap && p0 == 0 && !s_go) return;  // block-uniform
         for (int i = t; i < pn; i += kT) {
             const long long pg = (long long)ch.x + p0 + i;
             // through L2: in the single-kernel step the records were written
@@ -656,12 +624,45 @@ __device__ __forceinline__ void force_item(const ForceArgs &a, int item_index) {
     }
 }
 
+// Overlap mode: thread 0 waits until every field tile that holds a point of
+// this item's chunk carries the current stamp (the wait gives up after
+// kOverlapWaitNs of global time: kStatusTimeout, and the item adds nothing).
+// Deadlock-free under a programmatic launch, whose blocks are scheduled only
+// once every field block has started; after an ordinary launch the stamps
+// are all in place.
+constexpr unsigned long long kOverlapWaitNs = 500000000ull;
+__device__ __forceinline__ bool wait_item_tiles(const ForceArgs &a, int item_index) {
+    __shared__ int s_ok;
+    if (threadIdx.x == 0) {
+        const int4 item = a.items[item_index];
+        const WinDev W = a.win[item.x];
+        const int2 ch = a.chunks[item.w];
+        const unsigned int stamp = *a.ov_epoch + 1u;
+        const long long q0 = (long long)ch.x - W.point_off, q1 = q0 + ch.y - 1;
+        const int base = a.tile_base[item.x];
+        const int t1 = base + (int)(q1 / a.tile_pts);
+        int ok = 1;
+        const unsigned long long t_start = global_ns();
+        for (int tt = base + (int)(q0 / a.tile_pts); ok && tt <= t1; ++tt)
+            while (ld_acquire_u32(a.tile_flag + tt) != stamp) {
+                if (global_ns() - t_start > kOverlapWaitNs) {
+                    atomicOr(a.status, kStatusTimeout);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(128);
+            }
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
 template <bool LJ, int A, bool VOTE = false>
 __global__ void __launch_bounds__(ForceShape<A>::kThreads, VOTE ? 8 : ForceShape<A>::kMinBlocks)
     force_kernel(ForceArgs a) {
-    if (!a.overlap) pdl_wait();  // (overlap: each item waits for its own tiles)
+    if (!a.overlap) pdl_wait();
     pdl_trigger();
-    force_item<LJ, A, VOTE>(a, blockIdx.x);
+    if (!a.overlap || wait_item_tiles(a, blockIdx.x)) force_item<LJ, A, VOTE>(a, blockIdx.x);
 }
 
 // Forces of a field tile's own np points (records in shared memory) on every
