@@ -443,14 +443,16 @@ template <int S, bool GEN, bool RAW, bool VOTE, bool TMA = false>
 __global__ void __launch_bounds__(FieldShape<S>::kThreads) field_kernel(FieldArgs a) {
     pdl_wait();
     pdl_trigger();
+    // the stamp is read before the tile's work (kept in shared memory), so the
+    // block's exit does not wait on it
+    __shared__ unsigned int s_stamp;
+    if (a.tile_flag && threadIdx.x == 0) s_stamp = *a.ov_epoch + 1u;
     field_tile<S, GEN, RAW, VOTE, TMA>(a, blockIdx.x);
-    if (a.tile_flag) {  // the tile's records are written: stamp it for the force items
+    if (a.tile_flag) {
+        // the tile's records are written: the barrier orders every thread's
+        // stores before thread 0's release, which the force items acquire
         __syncthreads();
-        if (threadIdx.x == 0) {
-            const unsigned int stamp = *a.ov_epoch + 1u;
-            __threadfence();
-            st_release_u32(a.tile_flag + blockIdx.x, stamp);
-        }
+        if (threadIdx.x == 0) st_release_u32(a.tile_flag + blockIdx.x, s_stamp);
     }
 }
 
