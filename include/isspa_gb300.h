@@ -121,7 +121,8 @@ typedef struct isspa_engine_options {
                             groups of four with one warp vote per group (same results);
                             0 => per-pair branches */
     int integrator;      /* how isspa_step runs a step: 1 = bonded, umbrella and leapfrog
-                            kernels (bonded and umbrella concurrent with the IS-SPA pass);
+                            kernels (bonded, umbrella and nonbond on branches concurrent
+                            with the IS-SPA pass);
                             2 = one fused cooperative kernel for bonded, umbrella and
                             leapfrog after the force passes; 3 = the whole step in one
                             cooperative kernel (field, nonbond, bonded | force | update,

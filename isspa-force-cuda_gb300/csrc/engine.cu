@@ -1715,10 +1715,10 @@ int isspa_autotune(isspa_engine *e, int reps, int shape[ISSPA_SHAPE_COUNT]) {
             }
             e->set_nonbond_chunk(bestJ);
         }
-        // step integrator (unless fixed by the options): the separate bonded,
-        // umbrella and leapfrog kernels against the fused cooperative kernel,
-        // timed as single-step graph replays; positions, velocities and the
-        // step counter are restored afterwards
+        // step mode (the choices the options leave open): integrator,
+        // programmatic launches, fused field + force launch, force items on
+        // stamped field tiles, timed as single-step graph replays; positions,
+        // velocities and the step counter are restored afterwards
         ck(cudaMemsetAsync(e->facc, 0, 3 * sizeof(unsigned long long) * e->n_atoms, e->stream));
         const bool try_fused = e->opt.isspa_fused == 0 && e->fused_applies() &&
                                e->max_window_atoms() <= isspa_engine::kFusedMaxAtoms;
